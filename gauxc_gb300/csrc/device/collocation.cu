@@ -1,0 +1,124 @@
+// Collocation of basis functions (and their gradients) on the task grids.
+//
+// phi_mu(r_p) = R(|r_p - O|) * S_mu(r_p - O), R(r) = sum_k c_k exp(-a_k r^2),
+// grad phi = (r_p - O) R1 S + R grad S,  R1 = -2 sum_k a_k c_k exp(-a_k r^2)
+// (reference: collocation_device_masked_combined_kernel,
+//  kernels/collocation_masked_combined_kernels.hpp:26-92, and the gradient
+//  shell-to-task kernels kernels/collocation/collocation_shell_to_task_kernels_*).
+//
+// Output layout per task (batch scratch at scr + scr_off[t]): column-major
+// phi[col * npts_pad + p] (points fastest), followed by d/dx, d/dy, d/dz
+// blocks when gradients are requested.  Padding columns are written as zero.
+// One thread owns one point and walks the task's shell list, so every store
+// of a warp covers 32 consecutive points of one column.
+#include "device_common.cuh"
+#include "collocation_angular.inc"
+
+namespace gb300 {
+
+namespace {
+
+template <bool GRAD>
+__device__ __forceinline__ void eval_shell(int l, int pure, double x, double y, double z, double R,
+                                           double R1, double* f, double* fx, double* fy,
+                                           double* fz, int64_t s) {
+  if (GRAD) {
+    if (pure) {
+      switch (l) {
+        case 0: ang_grad_p_0(x, y, z, R, R1, f, fx, fy, fz, s); break;
+        case 1: ang_grad_p_1(x, y, z, R, R1, f, fx, fy, fz, s); break;
+        case 2: ang_grad_p_2(x, y, z, R, R1, f, fx, fy, fz, s); break;
+        case 3: ang_grad_p_3(x, y, z, R, R1, f, fx, fy, fz, s); break;
+        default: ang_grad_p_4(x, y, z, R, R1, f, fx, fy, fz, s); break;
+      }
+    } else {
+      switch (l) {
+        case 0: ang_grad_c_0(x, y, z, R, R1, f, fx, fy, fz, s); break;
+        case 1: ang_grad_c_1(x, y, z, R, R1, f, fx, fy, fz, s); break;
+        case 2: ang_grad_c_2(x, y, z, R, R1, f, fx, fy, fz, s); break;
+        case 3: ang_grad_c_3(x, y, z, R, R1, f, fx, fy, fz, s); break;
+        default: ang_grad_c_4(x, y, z, R, R1, f, fx, fy, fz, s); break;
+      }
+    }
+  } else {
+    if (pure) {
+      switch (l) {
+        case 0: ang_eval_p_0(x, y, z, R, f, s); break;
+        case 1: ang_eval_p_1(x, y, z, R, f, s); break;
+        case 2: ang_eval_p_2(x, y, z, R, f, s); break;
+        case 3: ang_eval_p_3(x, y, z, R, f, s); break;
+        default: ang_eval_p_4(x, y, z, R, f, s); break;
+      }
+    } else {
+      switch (l) {
+        case 0: ang_eval_c_0(x, y, z, R, f, s); break;
+        case 1: ang_eval_c_1(x, y, z, R, f, s); break;
+        case 2: ang_eval_c_2(x, y, z, R, f, s); break;
+        case 3: ang_eval_c_3(x, y, z, R, f, s); break;
+        default: ang_eval_c_4(x, y, z, R, f, s); break;
+      }
+    }
+  }
+}
+
+template <bool GRAD>
+__global__ void __launch_bounds__(128) collocation_kernel(ShellsDev sh, TasksDev tk,
+                                                          const int2* __restrict__ items,
+                                                          double* __restrict__ scr) {
+  const int2 it = items[blockIdx.x];
+  const int t = it.x;
+  const int p = it.y * blockDim.x + threadIdx.x;
+  const int np = tk.npts_pad[t];
+  if (p >= np) return;
+  const int64_t g = tk.pt_off[t] + p;
+  const double px = tk.x[g], py = tk.y[g], pz = tk.z[g];
+  const int64_t ld = np;
+  const int64_t blk = (int64_t)np * tk.nbe_pad[t];
+  double* f = scr + tk.scr_off[t];
+  double* fx = f + blk;
+  double* fy = fx + blk;
+  double* fz = fy + blk;
+  const int64_t s0 = tk.sh_off[t];
+  const int ns = tk.nsh[t];
+  for (int i = 0; i < ns; ++i) {
+    const int s = tk.sh_list[s0 + i];
+    const int col = tk.sh_col[s0 + i];
+    const double dx = px - sh.origin[3 * s + 0];
+    const double dy = py - sh.origin[3 * s + 1];
+    const double dz = pz - sh.origin[3 * s + 2];
+    const double r2 = dx * dx + dy * dy + dz * dz;
+    double R = 0., R1 = 0.;
+    for (int k = sh.prim_off[s]; k < sh.prim_off[s + 1]; ++k) {
+      const double a = sh.alpha[k];
+      const double e = sh.coeff[k] * exp(-a * r2);
+      R += e;
+      if (GRAD) R1 += a * e;
+    }
+    R1 *= -2.;
+    const int64_t o = (int64_t)col * ld + p;
+    eval_shell<GRAD>(sh.l[s], sh.pure[s], dx, dy, dz, R, R1, f + o, fx + o, fy + o, fz + o, ld);
+  }
+  for (int c = tk.nbe[t]; c < tk.nbe_pad[t]; ++c) {
+    const int64_t o = (int64_t)c * ld + p;
+    f[o] = 0.;
+    if (GRAD) {
+      fx[o] = 0.;
+      fy[o] = 0.;
+      fz[o] = 0.;
+    }
+  }
+}
+
+}  // namespace
+
+void launch_collocation(const ShellsDev& sh, const TasksDev& tk, const int2* items, int nitems,
+                        double* scr, bool grad, cudaStream_t s) {
+  if (nitems == 0) return;
+  if (grad)
+    collocation_kernel<true><<<nitems, 128, 0, s>>>(sh, tk, items, scr);
+  else
+    collocation_kernel<false><<<nitems, 128, 0, s>>>(sh, tk, items, scr);
+  GB300_CUDA(cudaGetLastError());
+}
+
+}  // namespace gb300

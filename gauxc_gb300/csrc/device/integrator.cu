@@ -1,0 +1,418 @@
+// Device-resident plan and the per-iteration stage loop of eval_exc_vxc.
+//
+// Reference driver: IncoreReplicatedXCDeviceIntegrator::eval_exc_vxc_ /
+// exc_vxc_local_work_ (src/xc_integrator/replicated/device/
+// incore_replicated_xc_device_integrator_exc_vxc.hpp:46-412):
+//   * dims checked (m == n == nbf, ld >= nbf), weights must be modified,
+//   * tasks sorted by npts * nbe (descending),
+//   * P sent to the device, EXC / N_el / VXC zeroed,
+//   * per task batch: collocation, X, vvars/uvars, functional, EXC/N_el,
+//     Z, VXC increment,
+//   * symmetrize, copy EXC / VXC back.
+// Differences by design: the plan (tasks, points, weights, shell->column maps,
+// work lists) is built once per load-balancer state and stays resident across
+// SCF iterations, so a call moves only P in and VXC out; every stage is a
+// single launch over all tasks of a batch, driven by precomputed work lists.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+#include "../host/device_api.hpp"
+#include "device_common.cuh"
+#include "functionals.cuh"
+#include "xc_kernels.cuh"
+#include "xc_mixed.cuh"
+
+namespace gb300 {
+
+int cuda_device_count() {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+namespace {
+
+int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
+
+// Device allocation from a caller buffer (bump) or cudaMalloc.
+class Arena {
+ public:
+  explicit Arena(RuntimeEnv* rt) : rt_(rt) {}
+  ~Arena() {
+    for (void* p : owned_) cudaFree(p);
+  }
+  template <typename T>
+  T* alloc(size_t n) {
+    const size_t bytes = std::max<size_t>(n * sizeof(T), 256);
+    if (rt_ && rt_->user_mem) {
+      const size_t off = (rt_->user_used + 255) / 256 * 256;
+      if (off + bytes > rt_->user_bytes)
+        throw error("device memory buffer given to the runtime environment is too small");
+      rt_->user_used = off + bytes;
+      return reinterpret_cast<T*>(static_cast<char*>(rt_->user_mem) + off);
+    }
+    void* p = nullptr;
+    GB300_CUDA(cudaMalloc(&p, bytes));
+    owned_.push_back(p);
+    return static_cast<T*>(p);
+  }
+  template <typename T>
+  T* upload(const std::vector<T>& v, cudaStream_t s) {
+    T* d = alloc<T>(v.size());
+    if (!v.empty())
+      GB300_CUDA(cudaMemcpyAsync(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    return d;
+  }
+
+ private:
+  RuntimeEnv* rt_;
+  std::vector<void*> owned_;
+};
+
+struct Batch {
+  int t_begin, t_end;
+  int coll_begin, coll_end;
+  int dens_begin, dens_end;
+  int vxc_begin, vxc_end;
+};
+
+}  // namespace
+
+class DeviceIntegrator {
+ public:
+  DeviceIntegrator(const LoadBalancer& lb, const XCFunctionalDesc& f, Precision prec,
+                   RuntimeEnv& rt)
+      : func_(f), prec_(prec), arena_(&rt), rt_(&rt) {
+    if (cuda_device_count() == 0) throw error("no CUDA device available for the device integrator");
+    GB300_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    for (auto& e : ev_) GB300_CUDA(cudaEventCreate(&e));
+    build(lb);
+  }
+  ~DeviceIntegrator() {
+    for (auto& e : ev_) cudaEventDestroy(e);
+    if (stream_) cudaStreamDestroy(stream_);
+  }
+
+  uint64_t generation = 0;
+  PlanStats stats;
+  std::map<std::string, double> timings;
+
+  void eval(const double* P, int64_t ldp, double* VXC, int64_t ldvxc, double* EXC, double* NEL,
+            bool den_only);
+
+ private:
+  void build(const LoadBalancer& lb);
+
+  XCFunctionalDesc func_;
+  Precision prec_;
+  Arena arena_;
+  RuntimeEnv* rt_;
+  cudaStream_t stream_ = nullptr;
+  cudaEvent_t ev_[4];
+
+  int nbf_ = 0;
+  bool gga_ = false;
+  ShellsDev sh_{};
+  TasksDev tk_{};
+  std::vector<Batch> batches_;
+  int2* coll_items_ = nullptr;
+  int2* dens_items_ = nullptr;
+  int4* vxc_items_ = nullptr;
+  int ndens_ = 0;
+  double* scr_ = nullptr;
+  double4* zcoef_ = nullptr;
+  double2* partials_ = nullptr;
+  double* P_ = nullptr;
+  double* A_ = nullptr;
+  double* V_ = nullptr;
+  double* out_ = nullptr;
+  MixedWorkspace mixed_{};
+};
+
+void DeviceIntegrator::build(const LoadBalancer& lb) {
+  const BasisSet& bs = *lb.basis;
+  nbf_ = bs.nbf;
+  gga_ = func_.is_gga != 0;
+  cudaStream_t s = stream_;
+
+  // ---- shells
+  {
+    std::vector<double> a, c, o;
+    std::vector<int> off{0}, l, pure;
+    for (const auto& sh : bs.shells) {
+      if (sh.l > 4) throw error("device collocation supports l <= 4");
+      for (int k = 0; k < sh.nprim; ++k) {
+        a.push_back(sh.alpha[k]);
+        c.push_back(sh.coeff[k]);
+      }
+      off.push_back((int)a.size());
+      o.insert(o.end(), sh.O, sh.O + 3);
+      l.push_back(sh.l);
+      pure.push_back(sh.pure);
+    }
+    sh_.nshells = (int)bs.shells.size();
+    sh_.alpha = arena_.upload(a, s);
+    sh_.coeff = arena_.upload(c, s);
+    sh_.prim_off = arena_.upload(off, s);
+    sh_.origin = arena_.upload(o, s);
+    sh_.l = arena_.upload(l, s);
+    sh_.pure = arena_.upload(pure, s);
+  }
+
+  // ---- task order: npts * nbe descending (stable)
+  const auto& tasks = lb.tasks;
+  std::vector<int> order(tasks.size());
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return (int64_t)tasks[a].npts * tasks[a].nbe > (int64_t)tasks[b].npts * tasks[b].nbe;
+  });
+
+  const int nt = (int)tasks.size();
+  std::vector<int64_t> pt_off(nt), bf_off(nt), sh_off(nt), scr_off(nt);
+  std::vector<int> npts_pad(nt), nbe(nt), nbe_pad(nt), nsh(nt);
+  std::vector<int> bf_list, sh_list, sh_col;
+  std::vector<double> X, Y, Z, W;
+  const int nblk = gga_ ? 5 : 2;
+  stats = PlanStats{};
+  int64_t pts = 0;
+  for (int i = 0; i < nt; ++i) {
+    const XCTask& t = tasks[order[i]];
+    pt_off[i] = pts;
+    npts_pad[i] = (int)round_up(t.npts, kPtBlock);
+    for (int p = 0; p < npts_pad[i]; ++p) {
+      const int q = p < t.npts ? p : 0;
+      X.push_back(t.points[3 * q + 0]);
+      Y.push_back(t.points[3 * q + 1]);
+      Z.push_back(t.points[3 * q + 2]);
+      W.push_back(p < t.npts ? t.weights[p] : 0.);
+    }
+    pts += npts_pad[i];
+    bf_off[i] = (int64_t)bf_list.size();
+    sh_off[i] = (int64_t)sh_list.size();
+    int col = 0;
+    for (int s_ : t.shell_list) {
+      sh_list.push_back(s_);
+      sh_col.push_back(col);
+      const int sz = bs.shells[s_].size();
+      for (int k = 0; k < sz; ++k) bf_list.push_back(bs.shell_offs[s_] + k);
+      col += sz;
+    }
+    nsh[i] = (int)t.shell_list.size();
+    nbe[i] = col;
+    if (col != t.nbe) throw error("task nbe does not match its shell list");
+    nbe_pad[i] = (int)round_up(col, kBfBlock);
+    for (int k = col; k < nbe_pad[i]; ++k) bf_list.push_back(-1);
+    stats.npts += t.npts;
+    stats.sum_npts_nbe += (double)t.npts * t.nbe;
+    stats.sum_npts_nbe2 += (double)t.npts * t.nbe * t.nbe;
+    stats.sum_pad_npts_nbe2 += (double)npts_pad[i] * nbe_pad[i] * nbe_pad[i];
+  }
+  stats.ntasks = nt;
+  stats.npts_pad = pts;
+
+  // ---- batches under the scratch budget
+  size_t free_b = 0, total_b = 0;
+  GB300_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  const double nbf2 = (double)nbf_ * nbf_ * 8.;
+  double static_bytes = 3 * nbf2 + pts * (4 * 8. + 32.) + bf_list.size() * 4. + 1e6;
+  double budget;
+  if (rt_->user_mem)
+    budget = (double)rt_->user_bytes - rt_->user_used - static_bytes - 64e6;
+  else
+    budget = rt_->fill_fraction * (double)free_b - static_bytes;
+  if (const char* cap = std::getenv("GAUXC_GB300_SCRATCH_GB")) budget = std::min(budget, atof(cap) * 1e9);
+  budget = std::min(budget, 128e9);
+  std::vector<int2> coll, dens;
+  std::vector<int4> vx;
+  double used = 0., max_used = 0.;
+  Batch cur{0, 0, 0, 0, 0, 0, 0, 0};
+  for (int i = 0; i < nt; ++i) {
+    const double need = (double)nblk * npts_pad[i] * nbe_pad[i] * 8.;
+    if (need > budget) throw error("insufficient device memory for one task's scratch");
+    if (used + need > budget && i > cur.t_begin) {
+      cur.t_end = i;
+      cur.coll_end = (int)coll.size();
+      cur.dens_end = (int)dens.size();
+      cur.vxc_end = (int)vx.size();
+      batches_.push_back(cur);
+      cur = Batch{i, i, (int)coll.size(), 0, (int)dens.size(), 0, (int)vx.size(), 0};
+      used = 0.;
+    }
+    scr_off[i] = (int64_t)(used / 8.);
+    used += need;
+    max_used = std::max(max_used, used);
+    for (int b = 0; b < (npts_pad[i] + 127) / 128; ++b) coll.push_back(make_int2(i, b));
+    for (int b = 0; b < npts_pad[i] / kPtBlock; ++b) dens.push_back(make_int2(i, b));
+    const int nb = nbe_pad[i] / kBfBlock;
+    for (int I = 0; I < nb; ++I)
+      for (int J = 0; J < nb; ++J) vx.push_back(make_int4(i, I, J, 0));
+  }
+  cur.t_end = nt;
+  cur.coll_end = (int)coll.size();
+  cur.dens_end = (int)dens.size();
+  cur.vxc_end = (int)vx.size();
+  if (nt > 0) batches_.push_back(cur);
+  stats.nbatches = (int64_t)batches_.size();
+  stats.scratch_bytes = max_used;
+
+  tk_.ntasks = nt;
+  tk_.pt_off = arena_.upload(pt_off, s);
+  tk_.npts_pad = arena_.upload(npts_pad, s);
+  tk_.nbe = arena_.upload(nbe, s);
+  tk_.nbe_pad = arena_.upload(nbe_pad, s);
+  tk_.bf_off = arena_.upload(bf_off, s);
+  tk_.bf_list = arena_.upload(bf_list, s);
+  tk_.sh_off = arena_.upload(sh_off, s);
+  tk_.nsh = arena_.upload(nsh, s);
+  tk_.sh_list = arena_.upload(sh_list, s);
+  tk_.sh_col = arena_.upload(sh_col, s);
+  tk_.scr_off = arena_.upload(scr_off, s);
+  tk_.x = arena_.upload(X, s);
+  tk_.y = arena_.upload(Y, s);
+  tk_.z = arena_.upload(Z, s);
+  tk_.w = arena_.upload(W, s);
+  coll_items_ = arena_.upload(coll, s);
+  dens_items_ = arena_.upload(dens, s);
+  vxc_items_ = arena_.upload(vx, s);
+  ndens_ = (int)dens.size();
+  scr_ = arena_.alloc<double>((size_t)(max_used / 8.) + 1);
+  zcoef_ = arena_.alloc<double4>(std::max<int64_t>(pts, 1));
+  partials_ = arena_.alloc<double2>(std::max(ndens_, 1));
+  P_ = arena_.alloc<double>((size_t)nbf_ * nbf_);
+  A_ = arena_.alloc<double>((size_t)nbf_ * nbf_);
+  V_ = arena_.alloc<double>((size_t)nbf_ * nbf_);
+  out_ = arena_.alloc<double>(2);
+  if (prec_ == Precision::Mixed) mixed_ = mixed_workspace_create(nt, npts_pad, nbe_pad, scr_off,
+                                                                 [&](size_t b) { return arena_.alloc<char>(b); });
+  GB300_CUDA(cudaStreamSynchronize(s));
+  generation = lb.generation;
+}
+
+void DeviceIntegrator::eval(const double* P, int64_t ldp, double* VXC, int64_t ldvxc, double* EXC,
+                            double* NEL, bool den_only) {
+  cudaStream_t s = stream_;
+  const size_t row = (size_t)nbf_ * sizeof(double);
+  auto t_host0 = std::chrono::steady_clock::now();
+  GB300_CUDA(cudaEventRecord(ev_[0], s));
+  GB300_CUDA(cudaMemcpy2DAsync(P_, row, P, (size_t)ldp * sizeof(double), row, nbf_,
+                               cudaMemcpyHostToDevice, s));
+  GB300_CUDA(cudaEventRecord(ev_[1], s));
+  const bool do_vxc = (VXC != nullptr) && !den_only;
+  if (do_vxc) GB300_CUDA(cudaMemsetAsync(A_, 0, (size_t)nbf_ * nbf_ * sizeof(double), s));
+  int64_t launches = 0;
+  for (const Batch& b : batches_) {
+    const int nt = b.t_end - b.t_begin;
+    launch_collocation(sh_, tk_, coll_items_ + b.coll_begin, b.coll_end - b.coll_begin, scr_, gga_, s);
+    ++launches;
+    if (prec_ == Precision::Mixed) {
+      launches += launch_density_mixed(mixed_, tk_, b.t_begin, b.t_end, dens_items_ + b.dens_begin,
+                                       b.dens_end - b.dens_begin, scr_, P_, nbf_, func_, zcoef_,
+                                       partials_ + b.dens_begin, s);
+    } else {
+      launch_density_fp64(tk_, dens_items_ + b.dens_begin, b.dens_end - b.dens_begin, scr_, P_,
+                          nbf_, func_, zcoef_, partials_ + b.dens_begin, s);
+      ++launches;
+    }
+    if (do_vxc) {
+      launch_zmat(tk_, b.t_begin, nt, zcoef_, scr_, gga_, s);
+      ++launches;
+      if (prec_ == Precision::Mixed) {
+        launches += launch_vxc_mixed(mixed_, tk_, b.t_begin, b.t_end, vxc_items_ + b.vxc_begin,
+                                     b.vxc_end - b.vxc_begin, scr_, A_, nbf_, gga_, s);
+      } else {
+        launch_vxc_fp64(tk_, vxc_items_ + b.vxc_begin, b.vxc_end - b.vxc_begin, scr_, A_, nbf_,
+                        gga_, s);
+        ++launches;
+      }
+    }
+  }
+  if (do_vxc) {
+    launch_symmetrize(A_, nbf_, V_, nbf_, s);
+    ++launches;
+  }
+  launch_reduce_partials(partials_, ndens_, out_, s);
+  ++launches;
+  GB300_CUDA(cudaEventRecord(ev_[2], s));
+  if (do_vxc)
+    GB300_CUDA(cudaMemcpy2DAsync(VXC, (size_t)ldvxc * sizeof(double), V_, row, row, nbf_,
+                                 cudaMemcpyDeviceToHost, s));
+  double en[2];
+  GB300_CUDA(cudaMemcpyAsync(en, out_, sizeof(en), cudaMemcpyDeviceToHost, s));
+  GB300_CUDA(cudaEventRecord(ev_[3], s));
+  GB300_CUDA(cudaStreamSynchronize(s));
+  auto t_host1 = std::chrono::steady_clock::now();
+  if (EXC) *EXC = en[0];
+  if (NEL) *NEL = en[1];
+  float h2d, comp, d2h;
+  GB300_CUDA(cudaEventElapsedTime(&h2d, ev_[0], ev_[1]));
+  GB300_CUDA(cudaEventElapsedTime(&comp, ev_[1], ev_[2]));
+  GB300_CUDA(cudaEventElapsedTime(&d2h, ev_[2], ev_[3]));
+  timings["h2d_ms"] = h2d;
+  timings["compute_ms"] = comp;
+  timings["d2h_ms"] = d2h;
+  timings["wall_ms"] = std::chrono::duration<double, std::milli>(t_host1 - t_host0).count();
+  stats.gpu_launches = launches;
+  timings["gpu_launches"] = (double)launches;
+}
+
+// ---------------------------------------------------------------- API glue
+
+namespace {
+void ensure_plan(XCIntegratorHandle& h) {
+  if (!h.lb) throw error("integrator has no load balancer");
+  if (!h.lb->weights_modified) throw error("Weights Have Not Been Modified");
+  if (!h.dev || h.dev->generation != h.lb->generation) {
+    h.dev.reset();
+    if (h.rt && h.rt->user_mem) h.rt->user_used = 0;
+    h.dev = std::make_shared<DeviceIntegrator>(*h.lb, *h.func, h.prec, *h.rt);
+  }
+}
+void check_dims(const XCIntegratorHandle& h, int64_t m, int64_t n, int64_t ldp) {
+  const int64_t nbf = h.lb->basis->nbf;
+  if (m != n) throw error("P Must Be Square");
+  if (m != nbf) throw error("P Must Have Same Dimension as Basis");
+  if (ldp < nbf) throw error("Invalid LDP");
+}
+}  // namespace
+
+void integrator_eval_exc_vxc(XCIntegratorHandle& h, int64_t m, int64_t n, const double* P,
+                             int64_t ldp, double* VXC, int64_t ldvxc, double* EXC) {
+  if (!P) throw error("null density matrix");
+  check_dims(h, m, n, ldp);
+  if (VXC && ldvxc < h.lb->basis->nbf) throw error("Invalid LDVXC");
+  ensure_plan(h);
+  double nel = 0.;
+  h.dev->eval(P, ldp, VXC, ldvxc, EXC, &nel, false);
+  h.last_exc = EXC ? *EXC : 0.;
+  h.last_nel = nel;
+}
+
+void integrator_integrate_den(XCIntegratorHandle& h, int64_t m, int64_t n, const double* P,
+                              int64_t ldp, double* NEL) {
+  if (!P) throw error("null density matrix");
+  check_dims(h, m, n, ldp);
+  ensure_plan(h);
+  double exc = 0., nel2 = 0.;
+  h.dev->eval(P, ldp, nullptr, 0, &exc, &nel2, true);
+  // the plan evaluates rho = 2 phi^T P phi (RKS, X factor 2); integrate_den
+  // integrates phi^T P phi (X factor 1, incore_..._integrate_den.hpp:133)
+  *NEL = 0.5 * nel2;
+  h.last_nel = *NEL;
+}
+
+std::map<std::string, double> integrator_timings(const XCIntegratorHandle& h) {
+  return h.dev ? h.dev->timings : std::map<std::string, double>{};
+}
+
+PlanStats integrator_plan_stats(XCIntegratorHandle& h) {
+  ensure_plan(h);
+  return h.dev->stats;
+}
+
+}  // namespace gb300

@@ -1,0 +1,78 @@
+// Symmetrization of the VXC accumulator and the EXC / N_el reduction.
+//
+// Reference: symmetrize_matrix_device (kernels/symmetrize_mat.cu:18-48) copies
+// the lower triangle to the upper one; here the accumulator holds A with
+// VXC = A + A^T, formed with a shared-memory tile transpose.  The reference
+// sums EXC / N_el with cublasDdot per batch (kernels/cublas_extensions.cu:
+// 86-112, plain FP64); this build reduces per-CTA partials in a fixed order
+// with Neumaier compensation, so the result is bit-reproducible.
+#include "xc_kernels.cuh"
+
+namespace gb300 {
+
+namespace {
+
+__global__ void symmetrize_kernel(const double* __restrict__ A, int n, double* __restrict__ V,
+                                  int64_t ld) {
+  __shared__ double tile[32][33];
+  const int bi = blockIdx.x * 32, bj = blockIdx.y * 32;
+  // load A(bj + ty, bi + tx) transposed into tile
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int row = bi + threadIdx.x, col = bj + r;
+    if (row < n && col < n) tile[r][threadIdx.x] = A[(int64_t)row * n + col];
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int row = bj + threadIdx.x, col = bi + r;  // element (row, col) of V, col-major
+    if (row < n && col < n)
+      V[(int64_t)col * ld + row] = A[(int64_t)col * n + row] + tile[threadIdx.x][r];
+  }
+}
+
+struct Neu {
+  double s = 0., c = 0.;
+  __device__ void add(double x) {
+    const double t = s + x;
+    if (fabs(s) >= fabs(x)) c += (s - t) + x;
+    else c += (x - t) + s;
+    s = t;
+  }
+  __device__ double value() const { return s + c; }
+};
+
+__global__ void reduce_partials_kernel(const double2* __restrict__ p, int64_t n, double* out) {
+  __shared__ double se[256], ce[256], sn[256], cn[256];
+  Neu e, q;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const double2 v = p[i];
+    e.add(v.x);
+    q.add(v.y);
+  }
+  se[threadIdx.x] = e.s; ce[threadIdx.x] = e.c;
+  sn[threadIdx.x] = q.s; cn[threadIdx.x] = q.c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    Neu E, N;
+    for (int i = 0; i < (int)blockDim.x; ++i) {
+      E.add(se[i]); E.add(ce[i]);
+      N.add(sn[i]); N.add(cn[i]);
+    }
+    out[0] = E.value();
+    out[1] = N.value();
+  }
+}
+
+}  // namespace
+
+void launch_symmetrize(const double* A, int nbf, double* vxc, int64_t ld, cudaStream_t s) {
+  dim3 g((nbf + 31) / 32, (nbf + 31) / 32), b(32, 8);
+  symmetrize_kernel<<<g, b, 0, s>>>(A, nbf, vxc, ld);
+  GB300_CUDA(cudaGetLastError());
+}
+
+void launch_reduce_partials(const double2* partials, int64_t n, double* out, cudaStream_t s) {
+  reduce_partials_kernel<<<1, 256, 0, s>>>(partials, n, out);
+  GB300_CUDA(cudaGetLastError());
+}
+
+}  // namespace gb300

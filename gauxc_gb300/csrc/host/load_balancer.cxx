@@ -1,0 +1,105 @@
+// Task generation with micro-batch shell screening and task merging.
+//
+// Follows src/load_balancer/host/replicated_host_load_balancer.cxx:22-193 and
+// the "petite" screen of petite_replicated_load_balancer.cxx:31-65:
+//   * for every atom, every batch of its (recentred) atomic grid gives one
+//     task candidate whose box is the bounding box of its points;
+//   * a shell is kept iff its cutoff sphere intersects the box;
+//   * candidates with no shells are dropped;
+//   * tasks are sorted by (iParent, shell_list) and tasks with identical
+//     (iParent, shell_list) are merged by concatenating their points.
+// Single-process build: every task is local (the reference's rank assignment
+// by XCTask::cost is the identity for one rank).
+#include "core.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <limits>
+
+namespace gb300 {
+
+namespace {
+
+std::vector<int32_t> screen_box(const BasisSet& bs, const double* lo, const double* up,
+                                int32_t& nbe) {
+  std::vector<int32_t> list;
+  nbe = 0;
+  for (size_t s = 0; s < bs.shells.size(); ++s) {
+    const Shell& sh = bs.shells[s];
+    if (cube_sphere_intersect(lo, up, sh.O, sh.cutoff_radius)) {
+      list.push_back((int32_t)s);
+      nbe += sh.size();
+    }
+  }
+  return list;
+}
+
+}  // namespace
+
+std::shared_ptr<LoadBalancer> make_load_balancer(std::shared_ptr<const Molecule> mol,
+                                                 std::shared_ptr<const MolGrid> mg,
+                                                 std::shared_ptr<const BasisSet> basis,
+                                                 bool device) {
+  auto lb = std::make_shared<LoadBalancer>();
+  lb->mol = mol;
+  lb->molgrid = mg;
+  lb->basis = basis;
+  lb->meta = std::make_shared<MolMeta>(*mol);
+  lb->device_screening = device;
+
+  std::vector<XCTask> tasks;
+  for (size_t iat = 0; iat < mol->size(); ++iat) {
+    const Atom& at = (*mol)[iat];
+    const double c[3] = {at.x, at.y, at.z};
+    const AtomicGrid& g = mg->grids.at(at.Z);
+    for (const auto& b : g.batches) {
+      const int64_t n = b.second - b.first;
+      if (n == 0) continue;
+      XCTask t;
+      t.iParent = (int32_t)iat;
+      t.npts = (int32_t)n;
+      t.points.resize(3 * n);
+      t.weights.resize(n);
+      double lo[3] = {std::numeric_limits<double>::infinity(),
+                      std::numeric_limits<double>::infinity(),
+                      std::numeric_limits<double>::infinity()};
+      double up[3] = {-lo[0], -lo[1], -lo[2]};
+      for (int64_t i = 0; i < n; ++i) {
+        for (int a = 0; a < 3; ++a) {
+          const double v = g.points[b.first + i][a] + c[a];
+          t.points[3 * i + a] = v;
+          lo[a] = std::min(lo[a], v);
+          up[a] = std::max(up[a], v);
+        }
+        t.weights[i] = g.weights[b.first + i];
+      }
+      t.shell_list = screen_box(*basis, lo, up, t.nbe);
+      if (t.shell_list.empty()) continue;
+      t.dist_nearest = lb->meta->dist_nearest[iat];
+      tasks.push_back(std::move(t));
+    }
+  }
+
+  std::stable_sort(tasks.begin(), tasks.end(), [](const XCTask& a, const XCTask& b) {
+    if (a.iParent != b.iParent) return a.iParent < b.iParent;
+    return a.shell_list < b.shell_list;
+  });
+
+  std::vector<XCTask> merged;
+  for (auto& t : tasks) {
+    if (!merged.empty() && merged.back().iParent == t.iParent &&
+        merged.back().shell_list == t.shell_list) {
+      XCTask& m = merged.back();
+      m.points.insert(m.points.end(), t.points.begin(), t.points.end());
+      m.weights.insert(m.weights.end(), t.weights.begin(), t.weights.end());
+      m.npts += t.npts;
+    } else {
+      merged.push_back(std::move(t));
+    }
+  }
+  lb->tasks = std::move(merged);
+  lb->generation++;
+  return lb;
+}
+
+}  // namespace gb300

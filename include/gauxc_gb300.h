@@ -1,0 +1,272 @@
+/*
+ * gauxc_gb300 -- C ABI of the GB300 device XC integrator.
+ *
+ * The first part mirrors the reference C API for the device XC-integration
+ * path: same type names, handle layout ({header, pointer}), function names,
+ * argument order and error behaviour (every call takes a GauXCStatus*; on
+ * failure status->code is non-zero and status->message holds a malloc'd
+ * string that gauxc_status_delete frees).  A code written against the
+ * reference headers (include/gauxc/c/*.h) links against this library for the
+ * functions below.  Each declaration cites the reference declaration it
+ * replaces.
+ *
+ * The second part (gauxc_gb300_*) holds extensions of this library: plan
+ * statistics, per-call timings, N_el of the last call, and stage-level entry
+ * points (SSF weights, collocation) that the parity tests call directly.
+ *
+ * Supported: RKS, LDA/GGA functionals SVWN5, PBE, revPBE, PBE0 (semilocal part),
+ * Mura-Knowles radial grids with Lebedev angular grids (unpruned, Robust and
+ * Treutler pruning), SSF partition weights on the device, shells with l <= 4.
+ */
+#ifndef GAUXC_GB300_H
+#define GAUXC_GB300_H
+
+#ifdef __cplusplus
+#include <cstddef>
+#include <cstdint>
+extern "C" {
+#else
+#include <stdbool.h>
+#include <stddef.h>
+#include <stdint.h>
+#endif
+
+/* ------------------------------------------------------------------ types */
+
+/* include/gauxc/c/status.h:24 */
+typedef struct GauXCStatus {
+  int code;
+  char* message;
+} GauXCStatus;
+
+/* include/gauxc/c/types.h:26 */
+enum GauXC_Type {
+  GauXC_Type_Molecule = 1,
+  GauXC_Type_BasisSet = 2,
+  GauXC_Type_MolGrid = 3,
+  GauXC_Type_RuntimeEnvironment = 4,
+  GauXC_Type_LoadBalancer = 5,
+  GauXC_Type_LoadBalancerFactory = 6,
+  GauXC_Type_MolecularWeights = 7,
+  GauXC_Type_MolecularWeightsFactory = 8,
+  GauXC_Type_Functional = 9,
+  GauXC_Type_Integrator = 10
+};
+
+/* include/gauxc/c/types.h:42 */
+typedef struct GauXCHeader {
+  enum GauXC_Type type;
+} GauXCHeader;
+
+/* include/gauxc/c/enums.h */
+enum GauXC_RadialQuad {
+  GauXC_RadialQuad_Becke,
+  GauXC_RadialQuad_MuraKnowles,
+  GauXC_RadialQuad_MurrayHandyLaming,
+  GauXC_RadialQuad_TreutlerAhlrichs
+};
+enum GauXC_AtomicGridSizeDefault {
+  GauXC_AtomicGridSizeDefault_FineGrid,
+  GauXC_AtomicGridSizeDefault_UltraFineGrid,
+  GauXC_AtomicGridSizeDefault_SuperFineGrid,
+  GauXC_AtomicGridSizeDefault_GM3,
+  GauXC_AtomicGridSizeDefault_GM5
+};
+enum GauXC_XCWeightAlg {
+  GauXC_XCWeightAlg_NOTPARTITIONED,
+  GauXC_XCWeightAlg_Becke,
+  GauXC_XCWeightAlg_SSF,
+  GauXC_XCWeightAlg_LKO
+};
+enum GauXC_ExecutionSpace { GauXC_ExecutionSpace_Host, GauXC_ExecutionSpace_Device };
+enum GauXC_PruningScheme {
+  GauXC_PruningScheme_Unpruned,
+  GauXC_PruningScheme_Robust,
+  GauXC_PruningScheme_Treutler
+};
+
+/* include/gauxc/c/functional.h:22-60 (subset; values keep the reference order) */
+enum GauXC_Functional {
+  GauXC_Functional_SVWN3,
+  GauXC_Functional_SVWN5,
+  GauXC_Functional_BLYP,
+  GauXC_Functional_B3LYP,
+  GauXC_Functional_PBE,
+  GauXC_Functional_revPBE,
+  GauXC_Functional_PBE0
+};
+
+/* include/gauxc/c/atom.h:32 */
+typedef struct GauXCAtom {
+  int64_t Z;
+  double x, y, z; /* bohr */
+} GauXCAtom;
+
+/* include/gauxc/c/shell.h:30 */
+typedef struct GauXCShell {
+  int32_t l;
+  bool pure;
+  int32_t nprim;
+  double exponents[32];
+  double coefficients[32];
+  double origin[3];
+  double shell_tolerance;
+} GauXCShell;
+
+/* handle types: include/gauxc/c/{molecule,basisset,molgrid,runtime_environment,
+   load_balancer,molecular_weights,functional,xc_integrator}.h */
+typedef struct GauXCMolecule { GauXCHeader hdr; void* ptr; } GauXCMolecule;
+typedef struct GauXCBasisSet { GauXCHeader hdr; void* ptr; } GauXCBasisSet;
+typedef struct GauXCMolGrid { GauXCHeader hdr; void* ptr; } GauXCMolGrid;
+typedef struct GauXCRuntimeEnvironment { GauXCHeader hdr; void* ptr; void* device_ptr; } GauXCRuntimeEnvironment;
+typedef struct GauXCLoadBalancer { GauXCHeader hdr; void* ptr; } GauXCLoadBalancer;
+typedef struct GauXCLoadBalancerFactory { GauXCHeader hdr; void* ptr; } GauXCLoadBalancerFactory;
+typedef struct GauXCMolecularWeights { GauXCHeader hdr; void* ptr; } GauXCMolecularWeights;
+typedef struct GauXCMolecularWeightsFactory { GauXCHeader hdr; void* ptr; } GauXCMolecularWeightsFactory;
+typedef struct GauXCFunctional { GauXCHeader hdr; void* ptr; } GauXCFunctional;
+typedef struct GauXCIntegrator { GauXCHeader hdr; void* ptr; } GauXCIntegrator;
+
+/* include/gauxc/c/molecular_weights.h:34 */
+typedef struct GauXCMolecularWeightsSettings {
+  enum GauXC_XCWeightAlg weight_alg;
+  bool becke_size_adjustment;
+} GauXCMolecularWeightsSettings;
+
+/* ------------------------------------------------------------------ reference C API */
+
+void gauxc_status_delete(GauXCStatus* status);                                   /* status.h:33 */
+void gauxc_object_delete(GauXCStatus* status, void** handle);                    /* types.h:55 */
+
+GauXCMolecule gauxc_molecule_new(GauXCStatus* status);                           /* molecule.h:45 */
+GauXCMolecule gauxc_molecule_new_from_atoms(GauXCStatus* status, const GauXCAtom* atoms,
+                                            size_t natoms);                      /* molecule.h:54 */
+void gauxc_molecule_delete(GauXCStatus* status, GauXCMolecule* mol);             /* molecule.h:61 */
+size_t gauxc_molecule_natoms(GauXCStatus* status, const GauXCMolecule mol);      /* molecule.h:69 */
+
+GauXCBasisSet gauxc_basisset_new(GauXCStatus* status);                           /* basisset.h:45 */
+GauXCBasisSet gauxc_basisset_new_from_shells(GauXCStatus* status, const GauXCShell* shells,
+                                             size_t nshells, bool normalize);    /* basisset.h:55 */
+void gauxc_basisset_delete(GauXCStatus* status, GauXCBasisSet* basis);           /* basisset.h:67 */
+
+GauXCMolGrid gauxc_molgrid_new_default(GauXCStatus* status, const GauXCMolecule mol,
+                                       enum GauXC_PruningScheme pruning_scheme,
+                                       int64_t batchsize,
+                                       enum GauXC_RadialQuad radial_quad,
+                                       enum GauXC_AtomicGridSizeDefault grid_size); /* molgrid.h:47 */
+void gauxc_molgrid_delete(GauXCStatus* status, GauXCMolGrid* molgrid);           /* molgrid.h:61 */
+
+GauXCRuntimeEnvironment gauxc_runtime_environment_new(GauXCStatus* status);      /* runtime_environment.h:45 */
+GauXCRuntimeEnvironment gauxc_device_runtime_environment_new(GauXCStatus* status,
+                                                             double fill_fraction); /* runtime_environment.h:89 */
+GauXCRuntimeEnvironment gauxc_device_runtime_environment_new_mem(GauXCStatus* status, void* mem,
+                                                                 size_t mem_sz); /* runtime_environment.h:103 */
+void gauxc_runtime_environment_delete(GauXCStatus* status, GauXCRuntimeEnvironment* env); /* runtime_environment.h:55 */
+int gauxc_runtime_environment_comm_rank(GauXCStatus* status, const GauXCRuntimeEnvironment env); /* runtime_environment.h:66 */
+int gauxc_runtime_environment_comm_size(GauXCStatus* status, const GauXCRuntimeEnvironment env); /* runtime_environment.h:76 */
+
+GauXCLoadBalancerFactory gauxc_load_balancer_factory_new(GauXCStatus* status,
+                                                         enum GauXC_ExecutionSpace ex,
+                                                         const char* kernel_name); /* load_balancer.h:69 */
+void gauxc_load_balancer_factory_delete(GauXCStatus* status, GauXCLoadBalancerFactory* f); /* load_balancer.h:80 */
+GauXCLoadBalancer gauxc_load_balancer_factory_get_instance(
+    GauXCStatus* status, const GauXCLoadBalancerFactory factory,
+    const GauXCRuntimeEnvironment env, const GauXCMolecule mol, const GauXCMolGrid mg,
+    const GauXCBasisSet basis);                                                   /* load_balancer.h:95 */
+void gauxc_load_balancer_delete(GauXCStatus* status, GauXCLoadBalancer* lb);     /* load_balancer.h:49 */
+
+GauXCMolecularWeightsFactory gauxc_molecular_weights_factory_new(
+    GauXCStatus* status, enum GauXC_ExecutionSpace ex, const char* local_work_kernel_name,
+    GauXCMolecularWeightsSettings settings);                                      /* molecular_weights.h:85 */
+void gauxc_molecular_weights_factory_delete(GauXCStatus* status,
+                                            GauXCMolecularWeightsFactory* factory); /* molecular_weights.h:97 */
+GauXCMolecularWeights gauxc_molecular_weights_factory_get_instance(
+    GauXCStatus* status, const GauXCMolecularWeightsFactory factory);             /* molecular_weights.h:108 */
+void gauxc_molecular_weights_modify_weights(GauXCStatus* status, const GauXCMolecularWeights mw,
+                                            const GauXCLoadBalancer lb);          /* molecular_weights.h:63 */
+void gauxc_molecular_weights_delete(GauXCStatus* status, GauXCMolecularWeights* mw); /* molecular_weights.h:52 */
+
+GauXCFunctional gauxc_functional_from_string(GauXCStatus* status, const char* functional_spec,
+                                             bool polarized);                    /* functional.h:359 */
+GauXCFunctional gauxc_functional_from_enum(GauXCStatus* status,
+                                           enum GauXC_Functional functional_type,
+                                           bool polarized);                      /* functional.h:372 */
+void gauxc_functional_delete(GauXCStatus* status, GauXCFunctional* functional);  /* functional.h:383 */
+
+GauXCIntegrator gauxc_integrator_new(GauXCStatus* status, const GauXCFunctional functional,
+                                     const GauXCLoadBalancer lb,
+                                     enum GauXC_ExecutionSpace execution_space,
+                                     const char* integrator_input_type,
+                                     const char* integrator_kernel_name,
+                                     const char* local_work_kernel_name,
+                                     const char* reduction_kernel_name);         /* xc_integrator.h:61 */
+void gauxc_integrator_delete(GauXCStatus* status, GauXCIntegrator* integrator);  /* xc_integrator.h:44 */
+void gauxc_integrator_integrate_den(GauXCStatus* status, const GauXCIntegrator integrator,
+                                    const int64_t m, const int64_t n,
+                                    const double* density_matrix, const int64_t ldp,
+                                    double* den);                                 /* xc_integrator.h:82 */
+void gauxc_integrator_eval_exc_rks(GauXCStatus* status, const GauXCIntegrator integrator,
+                                   const int64_t m, const int64_t n,
+                                   const double* density_matrix, const int64_t ldp,
+                                   double* exc);                                  /* xc_integrator.h:102 */
+void gauxc_integrator_eval_exc_vxc_rks(GauXCStatus* status, const GauXCIntegrator integrator,
+                                       const int64_t m, const int64_t n,
+                                       const double* density_matrix, const int64_t ldp,
+                                       double* exc, double* vxc_matrix,
+                                       const int64_t vxc_ld);                     /* xc_integrator.h:180 */
+
+/* ------------------------------------------------------------------ extensions */
+
+/* Library version string (static storage). */
+const char* gauxc_gb300_version(void);
+/* Number of CUDA devices visible (0 on a machine without GPU). */
+int gauxc_gb300_device_count(void);
+
+size_t gauxc_gb300_basisset_nshells(GauXCStatus* status, const GauXCBasisSet basis);
+int32_t gauxc_gb300_basisset_nbf(GauXCStatus* status, const GauXCBasisSet basis);
+/* Shell i after normalization; shell_tolerance holds the tolerance, *cutoff the radius. */
+void gauxc_gb300_basisset_get_shell(GauXCStatus* status, const GauXCBasisSet basis, size_t i,
+                                    GauXCShell* out, double* cutoff_radius);
+/* Reset the screening tolerance of every shell (recomputes cutoff radii). */
+void gauxc_gb300_basisset_set_tolerance(GauXCStatus* status, GauXCBasisSet basis, double tol);
+
+/* Atomic grid of element Z (origin-centred, batch order). Pass null arrays to query sizes. */
+void gauxc_gb300_molgrid_atomic_grid(GauXCStatus* status, const GauXCMolGrid mg, int64_t Z,
+                                     int64_t* npts, int64_t* nbatches, double* points,
+                                     double* weights, int64_t* batch_ranges);
+
+size_t gauxc_gb300_load_balancer_ntasks(GauXCStatus* status, const GauXCLoadBalancer lb);
+/* info = {iParent, npts, nbe, nshells}; *dist_nearest of the task's parent atom. */
+void gauxc_gb300_load_balancer_task_info(GauXCStatus* status, const GauXCLoadBalancer lb,
+                                         size_t i, int32_t info[4], double* dist_nearest);
+/* points (3*npts, xyz interleaved), weights (npts), shell_list (nshells); any may be null. */
+void gauxc_gb300_load_balancer_task_data(GauXCStatus* status, const GauXCLoadBalancer lb,
+                                         size_t i, double* points, double* weights,
+                                         int32_t* shell_list);
+bool gauxc_gb300_load_balancer_weights_modified(GauXCStatus* status, const GauXCLoadBalancer lb);
+
+/* N_el (integral of the total density) of the last eval_exc_vxc call. */
+double gauxc_gb300_integrator_last_nel(GauXCStatus* status, const GauXCIntegrator integrator);
+/* Timings of the last call in ms: {h2d, compute, d2h, wall}; returns the count written. */
+int gauxc_gb300_integrator_timings(GauXCStatus* status, const GauXCIntegrator integrator,
+                                   double* out, int nmax);
+/* Plan statistics: {ntasks, npts, npts_pad, nbatches, sum npts*nbe, sum npts*nbe^2,
+   sum npts_pad*nbe_pad^2, scratch bytes, kernel launches of the last call}. */
+int gauxc_gb300_integrator_plan_stats(GauXCStatus* status, const GauXCIntegrator integrator,
+                                      double* out, int nmax);
+
+/* Stage entry points (host arrays, computed on the device).
+   SSF weights, reference kernel cuda_ssf_1d.cu:24-144 (partition_weights_ssf_1d). */
+void gauxc_gb300_ssf_weights(GauXCStatus* status, int64_t npts, int32_t natoms,
+                             const double* points, const int32_t* iparent,
+                             const double* dist_nearest, const double* coords,
+                             double* weights);
+/* Collocation of the listed shells, host layout eval[ipt*nbe + ibf]; gradients
+   when dphi_* are non-null.  Reference: collocation_device.cu (eval_collocation*). */
+void gauxc_gb300_collocation(GauXCStatus* status, const GauXCBasisSet basis, int64_t npts,
+                             const double* points, int32_t nshells, const int32_t* shell_list,
+                             double* phi, double* dphi_x, double* dphi_y, double* dphi_z);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GAUXC_GB300_H */

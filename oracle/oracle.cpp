@@ -1,0 +1,505 @@
+// CPU oracle for the XC integration path -- TEST INFRASTRUCTURE ONLY.
+//
+// This file restates, on the CPU and in plain FP64, the reference host
+// algorithm that the GB300 device path must reproduce.  Only the tests, the
+// smoke check and the CPU-baseline leg of bench.py load it; the library in
+// gauxc_gb300/ never links or calls it.
+//
+// Restated reference code (paths inside the GauXC source tree):
+//   shell normalization        include/gauxc/shell.hpp:72-109
+//   shell cutoff radius        include/gauxc/util/gau_rad_eval.hpp:32-71
+//   SSF weights (host)         src/xc_integrator/local_work_driver/host/reference/weights.cxx:117-237
+//   per-task integration       src/xc_integrator/replicated/host/
+//                              reference_replicated_xc_host_integrator_exc_vxc.hpp:106-601
+//   X = fac * P_sub * B         src/xc_integrator/local_work_driver/host/reference_local_host_work_driver.cxx:123-146
+//   rho / grad rho / gamma     same file :150-163, :242-268
+//   Z (LDA / GGA)              same file :586-604, :678-713
+//   VXC += syr2k + scatter     same file :1672-1692; submatrix helpers host/util.hpp:22-194
+// Collocation (the reference uses gau2grid on the host) is evaluated from the
+// closed-form real solid harmonics (Helgaker, Jorgensen, Olsen, eqs.
+// 6.4.47-6.4.50) as explicit monomial sums; cartesian shells are monomials.
+// Functionals: Slater, VWN (paramagnetic, RPA-fit parameters), PW92, PBE x/c from the original
+// papers; vrho / vsigma come from forward-mode dual numbers, independent of
+// the hand-derived derivatives used on the device.  Density thresholds equal
+// the device ones (1e-15; 1e-12 for PBE correlation).
+#include <omp.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+namespace {
+
+// ------------------------------------------------------------------ duals
+struct D {
+  double v, r, s;  // value, d/drho, d/dsigma
+};
+inline D mk(double v) { return {v, 0., 0.}; }
+inline D operator+(D a, D b) { return {a.v + b.v, a.r + b.r, a.s + b.s}; }
+inline D operator-(D a, D b) { return {a.v - b.v, a.r - b.r, a.s - b.s}; }
+inline D operator*(D a, D b) { return {a.v * b.v, a.r * b.v + a.v * b.r, a.s * b.v + a.v * b.s}; }
+inline D operator/(D a, D b) {
+  const double i = 1. / b.v;
+  return {a.v * i, (a.r * b.v - a.v * b.r) * i * i, (a.s * b.v - a.v * b.s) * i * i};
+}
+inline D operator+(D a, double b) { return {a.v + b, a.r, a.s}; }
+inline D operator+(double b, D a) { return {a.v + b, a.r, a.s}; }
+inline D operator-(D a, double b) { return {a.v - b, a.r, a.s}; }
+inline D operator-(double b, D a) { return {b - a.v, -a.r, -a.s}; }
+inline D operator*(D a, double b) { return {a.v * b, a.r * b, a.s * b}; }
+inline D operator*(double b, D a) { return {a.v * b, a.r * b, a.s * b}; }
+inline D operator/(D a, double b) { return {a.v / b, a.r / b, a.s / b}; }
+inline D operator/(double b, D a) { return mk(b) / a; }
+inline D operator-(D a) { return {-a.v, -a.r, -a.s}; }
+inline D chain(D a, double f, double df) { return {f, df * a.r, df * a.s}; }
+inline D dlog(D a) { return chain(a, std::log(a.v), 1. / a.v); }
+inline D dexp(D a) { const double e = std::exp(a.v); return chain(a, e, e); }
+inline D dsqrt(D a) { const double q = std::sqrt(a.v); return chain(a, q, 0.5 / q); }
+inline D datan(D a) { return chain(a, std::atan(a.v), 1. / (1. + a.v * a.v)); }
+inline D dpow(D a, double p) { return chain(a, std::pow(a.v, p), p * std::pow(a.v, p - 1.)); }
+
+const double PI = 3.14159265358979323846;
+
+// per-volume energy densities rho*eps
+D slater(D rho) { return -0.75 * std::pow(3. / PI, 1. / 3.) * dpow(rho, 4. / 3.); }
+
+// VWN correlation with the RPA-fit paramagnetic parameters; this is the
+// parameter set that reproduces the reference's SVWN5 goldens
+// (tests/ref_data/benzene_svwn5_cc-pvdz_ufg_ssf*.hdf5) to 1e-12.
+D vwn5(D rho) {
+  const double A = 0.0310907, b = 13.0720, c = 42.7198, x0 = -0.409286;
+  const double Q = std::sqrt(4 * c - b * b);
+  const double X0 = x0 * x0 + b * x0 + c;
+  D rs = dpow(3. / (4. * PI * rho), 1. / 3.);
+  D x = dsqrt(rs);
+  D X = x * x + b * x + c;
+  D at = datan(Q / (2. * x + b));
+  D e = A * (dlog(x * x / X) + (2. * b / Q) * at -
+             (b * x0 / X0) * (dlog((x - x0) * (x - x0) / X) + (2. * (b + 2. * x0) / Q) * at));
+  return rho * e;
+}
+
+D pw92(D rs) {
+  const double A = 0.0310907, a1 = 0.21370, b1 = 7.5957, b2 = 3.5876, b3 = 1.6382, b4 = 0.49294;
+  D s = dsqrt(rs);
+  D den = 2. * A * (b1 * s + b2 * rs + b3 * rs * s + b4 * rs * rs);
+  return -2. * A * (1. + a1 * rs) * dlog(1. + 1. / den);
+}
+
+D pbe_x(D rho, D sigma, double kappa, double mu) {
+  D kf = dpow(3. * PI * PI * rho, 1. / 3.);
+  D s2 = sigma / (4. * kf * kf * rho * rho);
+  D F = 1. + kappa - kappa / (1. + mu * s2 / kappa);
+  return slater(rho) * F;
+}
+
+D pbe_c(D rho, D sigma) {
+  const double beta = 0.06672455060314922;
+  const double gamma = (1. - std::log(2.)) / (PI * PI);
+  D rs = dpow(3. / (4. * PI * rho), 1. / 3.);
+  D ec = pw92(rs);
+  D kf = dpow(3. * PI * PI * rho, 1. / 3.);
+  D ks = dsqrt(4. * kf / PI);
+  D t2 = sigma / (4. * ks * ks * rho * rho);
+  D A = (beta / gamma) / (dexp(-1. * ec / gamma) - 1.);
+  D At2 = A * t2;
+  D H = gamma * dlog(1. + (beta / gamma) * t2 * (1. + At2) / (1. + At2 + At2 * At2));
+  return rho * (ec + H);
+}
+
+struct Func {
+  int kind;  // 0 = SVWN5, 1 = PBE family
+  double xs, cs, kappa, mu;
+};
+
+void eval_functional(const Func& f, double rho, double sigma, double& eps, double& vr,
+                     double& vs) {
+  D r{rho, 1., 0.}, s{sigma, 0., 1.};
+  D e = mk(0.);
+  if (f.kind == 0) {
+    if (rho > 1e-15) e = e + f.xs * slater(r);
+    if (rho > 1e-15) e = e + f.cs * vwn5(r);
+  } else {
+    if (rho > 1e-15) e = e + f.xs * pbe_x(r, s, f.kappa, f.mu);
+    if (rho > 1e-12) e = e + f.cs * pbe_c(r, s);
+  }
+  eps = rho > 0. && e.v != 0. ? e.v / rho : 0.;
+  vr = e.r;
+  vs = e.s;
+}
+
+// ------------------------------------------------------------------ shells
+struct Mono {
+  double c;
+  int a, b, z;
+};
+
+double fact(int n) {
+  double r = 1.;
+  for (int i = 2; i <= n; ++i) r *= i;
+  return r;
+}
+double binom(int n, int k) {
+  if (k < 0 || k > n) return 0.;
+  return fact(n) / (fact(k) * fact(n - k));
+}
+
+// Real solid harmonic S_lm as monomials (Racah normalization).
+std::vector<Mono> solid_harmonic(int l, int m) {
+  const int am = std::abs(m);
+  const int odd = m >= 0 ? 0 : 1;
+  const double N = std::sqrt(2. * fact(l + am) * fact(l - am) / (m == 0 ? 2. : 1.)) /
+                   (std::pow(2., am) * fact(l));
+  std::vector<Mono> out;
+  for (int t = 0; t <= (l - am) / 2; ++t)
+    for (int u = 0; u <= t; ++u)
+      for (int tv = odd; tv <= am; tv += 2) {
+        const double sign = ((t + (tv - odd) / 2) % 2) ? -1. : 1.;
+        const double c = sign * std::pow(0.25, t) * binom(l, t) * binom(l - t, am + t) *
+                         binom(t, u) * binom(am, tv);
+        const int px = 2 * t + am - 2 * u - tv, py = 2 * u + tv, pz = l - 2 * t - am;
+        bool merged = false;
+        for (auto& mo : out)
+          if (mo.a == px && mo.b == py && mo.z == pz) {
+            mo.c += N * c;
+            merged = true;
+          }
+        if (!merged) out.push_back({N * c, px, py, pz});
+      }
+  return out;
+}
+
+std::vector<std::vector<Mono>> angular_set(int l, bool pure) {
+  std::vector<std::vector<Mono>> fs;
+  if (pure) {
+    for (int m = -l; m <= l; ++m) fs.push_back(solid_harmonic(l, m));
+  } else {
+    for (int a = l; a >= 0; --a)
+      for (int b = l - a; b >= 0; --b) fs.push_back({{1., a, b, l - a - b}});
+  }
+  return fs;
+}
+
+inline double ipow(double x, int n) {
+  double r = 1.;
+  for (int i = 0; i < n; ++i) r *= x;
+  return r;
+}
+
+double mono_eval(const std::vector<Mono>& ms, double x, double y, double z) {
+  double s = 0.;
+  for (const auto& m : ms) s += m.c * ipow(x, m.a) * ipow(y, m.b) * ipow(z, m.z);
+  return s;
+}
+double mono_deriv(const std::vector<Mono>& ms, int axis, double x, double y, double z) {
+  double s = 0.;
+  for (const auto& m : ms) {
+    int p[3] = {m.a, m.b, m.z};
+    if (p[axis] == 0) continue;
+    const double f = m.c * p[axis];
+    p[axis] -= 1;
+    s += f * ipow(x, p[0]) * ipow(y, p[1]) * ipow(z, p[2]);
+  }
+  return s;
+}
+
+struct Basis {
+  int nshells;
+  const int32_t* l;
+  const int32_t* pure;
+  const int32_t* nprim;
+  const double* alpha;  // [nshells*32]
+  const double* coeff;  // [nshells*32]
+  const double* origin; // [3*nshells]
+  std::vector<int> ao_off;
+  std::vector<std::vector<std::vector<Mono>>> ang;
+  Basis(int n, const int32_t* l_, const int32_t* p_, const int32_t* np_, const double* a_,
+        const double* c_, const double* o_)
+      : nshells(n), l(l_), pure(p_), nprim(np_), alpha(a_), coeff(c_), origin(o_) {
+    int off = 0;
+    for (int s = 0; s < n; ++s) {
+      ao_off.push_back(off);
+      ang.push_back(angular_set(l[s], pure[s] != 0));
+      off += (int)ang.back().size();
+    }
+    ao_off.push_back(off);
+  }
+  int size(int s) const { return (int)ang[s].size(); }
+};
+
+// host layout: out[ipt*nbe + ibf]
+void collocate(const Basis& B, int npts, const double* pts, int nsh, const int32_t* shells,
+               int nbe, double* f, double* fx, double* fy, double* fz) {
+  for (int p = 0; p < npts; ++p) {
+    int col = 0;
+    for (int i = 0; i < nsh; ++i) {
+      const int s = shells[i];
+      const double x = pts[3 * p] - B.origin[3 * s];
+      const double y = pts[3 * p + 1] - B.origin[3 * s + 1];
+      const double z = pts[3 * p + 2] - B.origin[3 * s + 2];
+      const double r2 = x * x + y * y + z * z;
+      double R = 0., R1 = 0.;
+      for (int k = 0; k < B.nprim[s]; ++k) {
+        const double a = B.alpha[32 * s + k];
+        const double e = B.coeff[32 * s + k] * std::exp(-a * r2);
+        R += e;
+        R1 += -2. * a * e;
+      }
+      for (const auto& ms : B.ang[s]) {
+        const double S = mono_eval(ms, x, y, z);
+        const size_t o = (size_t)p * nbe + col;
+        f[o] = R * S;
+        if (fx) {
+          fx[o] = R1 * x * S + R * mono_deriv(ms, 0, x, y, z);
+          fy[o] = R1 * y * S + R * mono_deriv(ms, 1, x, y, z);
+          fz[o] = R1 * z * S + R * mono_deriv(ms, 2, x, y, z);
+        }
+        ++col;
+      }
+    }
+  }
+}
+
+// C[m x n] = alpha * A[m x k] * op(B) (+ beta C), column-major.
+// op(B) = B [k x n] (ldb) when !bt, else B^T with B [n x k].
+void gemm(int m, int n, int k, double alpha, const double* A, int lda, const double* Bm, int ldb,
+          bool bt, double* C, int ldc) {
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < m; ++i) C[(size_t)j * ldc + i] = 0.;
+  const int NB = 8, KB = 128;
+  for (int k0 = 0; k0 < k; k0 += KB) {
+    const int k1 = std::min(k, k0 + KB);
+    for (int j0 = 0; j0 < n; j0 += NB) {
+      const int j1 = std::min(n, j0 + NB);
+      for (int j = j0; j < j1; ++j) {
+        double* c = C + (size_t)j * ldc;
+        for (int kk = k0; kk < k1; ++kk) {
+          const double b = bt ? Bm[(size_t)kk * ldb + j] : Bm[(size_t)j * ldb + kk];
+          if (b == 0.) continue;
+          const double ab = alpha * b;
+          const double* a = A + (size_t)kk * lda;
+#pragma omp simd
+          for (int i = 0; i < m; ++i) c[i] += ab * a[i];
+        }
+      }
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+// --------------------------------------------------------------- shells
+void oracle_normalize_shell(int l, int nprim, const double* alpha, double* coeff) {
+  const double sqrt_pi3 = 5.56832799683170784528481798212;
+  double dfact = 1.;
+  for (int k = 2 * l - 1; k > 1; k -= 2) dfact *= k;
+  const double df = std::pow(2., l) / sqrt_pi3 / dfact;
+  for (int i = 0; i < nprim; ++i)
+    if (alpha[i] != 0.) {
+      const double ta = 2. * alpha[i];
+      coeff[i] *= std::sqrt(df * (std::pow(ta, l + 1) * std::sqrt(ta)));
+    }
+  double s = 0.;
+  for (int i = 0; i < nprim; ++i)
+    for (int j = 0; j <= i; ++j) {
+      const double g = alpha[i] + alpha[j];
+      s += (i == j ? 1 : 2) * coeff[i] * coeff[j] / (df * (std::pow(g, l + 1) * std::sqrt(g)));
+    }
+  const double f = 1. / std::sqrt(s);
+  for (int i = 0; i < nprim; ++i) coeff[i] *= f;
+}
+
+// --------------------------------------------------------------- SSF (host algorithm)
+void oracle_ssf_weights(int64_t npts, int natoms, const double* pts, const int32_t* iparent,
+                        const double* dist_nearest, const double* coords, double* weights,
+                        int nthreads) {
+  const double a = 0.64, tol = 1e-13;
+  std::vector<double> rab((size_t)natoms * natoms, 0.);
+  for (int i = 0; i < natoms; ++i)
+    for (int j = 0; j < natoms; ++j) {
+      const double dx = coords[3 * i] - coords[3 * j], dy = coords[3 * i + 1] - coords[3 * j + 1],
+                   dz = coords[3 * i + 2] - coords[3 * j + 2];
+      rab[(size_t)i * natoms + j] = std::sqrt(dx * dx + dy * dy + dz * dz);
+    }
+  auto g = [&](double x) {
+    const double s = x / a, s2 = s * s, s3 = s * s2, s5 = s3 * s2, s7 = s5 * s2;
+    return (35. * (s - s3) + 21. * s5 - 5. * s7) / 16.;
+  };
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel
+  {
+    std::vector<double> P(natoms), r(natoms);
+#pragma omp for schedule(dynamic, 256)
+    for (int64_t p = 0; p < npts; ++p) {
+      const int ip = iparent[p];
+      const double cut = 0.5 * (1. - a) * dist_nearest[p];
+      for (int A = 0; A < natoms; ++A) {
+        const double dx = pts[3 * p] - coords[3 * A], dy = pts[3 * p + 1] - coords[3 * A + 1],
+                     dz = pts[3 * p + 2] - coords[3 * A + 2];
+        r[A] = std::sqrt(dx * dx + dy * dy + dz * dz);
+      }
+      if (r[ip] < cut) continue;
+      std::fill(P.begin(), P.end(), 1.);
+      for (int iA = 0; iA < natoms; ++iA)
+        for (int jA = 0; jA < iA; ++jA)
+          if (P[iA] > tol || P[jA] > tol) {
+            const double mu = (r[iA] - r[jA]) / rab[(size_t)jA + (size_t)iA * natoms];
+            if (mu <= -a) P[jA] = 0.;
+            else if (mu >= a) P[iA] = 0.;
+            else {
+              const double s = 0.5 * (1. - g(mu));
+              P[iA] *= s;
+              P[jA] *= 1. - s;
+            }
+          }
+      double sum = 0.;
+      for (int A = 0; A < natoms; ++A) sum += P[A];
+      weights[p] *= P[ip] / sum;
+    }
+  }
+}
+
+// --------------------------------------------------------------- collocation
+void oracle_collocation(int nshells_basis, const int32_t* l, const int32_t* pure,
+                        const int32_t* nprim, const double* alpha, const double* coeff,
+                        const double* origin, int npts, const double* pts, int nsh,
+                        const int32_t* shell_list, int grad, double* f, double* fx, double* fy,
+                        double* fz) {
+  Basis B(nshells_basis, l, pure, nprim, alpha, coeff, origin);
+  int nbe = 0;
+  for (int i = 0; i < nsh; ++i) nbe += B.size(shell_list[i]);
+  collocate(B, npts, pts, nsh, shell_list, nbe, f, grad ? fx : nullptr, grad ? fy : nullptr,
+            grad ? fz : nullptr);
+}
+
+// --------------------------------------------------------------- functional
+void oracle_functional(int kind, double xs, double cs, double kappa, double mu, int64_t npts,
+                       const double* rho, const double* sigma, double* eps, double* vrho,
+                       double* vsigma) {
+  const Func f{kind, xs, cs, kappa, mu};
+  for (int64_t i = 0; i < npts; ++i) {
+    double e, vr, vs;
+    eval_functional(f, rho[i], sigma ? sigma[i] : 0., e, vr, vs);
+    eps[i] = e;
+    vrho[i] = vr;
+    if (vsigma) vsigma[i] = vs;
+  }
+}
+
+// --------------------------------------------------------------- integrator
+// Tasks: task t owns points [pt_off[t], pt_off[t+1]) and shells
+// [sh_off[t], sh_off[t+1]) of shell_list.  P and VXC are nbf x nbf
+// column-major (ld = nbf).  Returns EXC and N_el through exc_nel[2].
+void oracle_eval_exc_vxc(int nshells_basis, const int32_t* l, const int32_t* pure,
+                         const int32_t* nprim, const double* alpha, const double* coeff,
+                         const double* origin, int nbf, int ntasks, const int64_t* pt_off,
+                         const double* pts, const double* wts, const int64_t* sh_off,
+                         const int32_t* shell_list, int kind, double xs, double cs, double kappa,
+                         double mu, int gga, const double* P, double* VXC, double* exc_nel,
+                         int nthreads) {
+  Basis B(nshells_basis, l, pure, nprim, alpha, coeff, origin);
+  const Func func{kind, xs, cs, kappa, mu};
+  if (VXC) std::memset(VXC, 0, sizeof(double) * (size_t)nbf * nbf);
+  double EXC = 0., NEL = 0.;
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel reduction(+ : EXC, NEL)
+  {
+    std::vector<double> f, fx, fy, fz, Ps, X, Zm, V, rho, gxv, gyv, gzv;
+#pragma omp for schedule(dynamic, 1)
+    for (int t = 0; t < ntasks; ++t) {
+      const int npts = (int)(pt_off[t + 1] - pt_off[t]);
+      const int nsh = (int)(sh_off[t + 1] - sh_off[t]);
+      const int32_t* sl = shell_list + sh_off[t];
+      const double* tp = pts + 3 * pt_off[t];
+      const double* tw = wts + pt_off[t];
+      std::vector<int> bf;
+      for (int i = 0; i < nsh; ++i)
+        for (int k = 0; k < B.size(sl[i]); ++k) bf.push_back(B.ao_off[sl[i]] + k);
+      const int nbe = (int)bf.size();
+      const size_t ne = (size_t)npts * nbe;
+      f.assign(ne, 0.);
+      if (gga) {
+        fx.assign(ne, 0.);
+        fy.assign(ne, 0.);
+        fz.assign(ne, 0.);
+      }
+      collocate(B, npts, tp, nsh, sl, nbe, f.data(), gga ? fx.data() : nullptr,
+                gga ? fy.data() : nullptr, gga ? fz.data() : nullptr);
+      // submatrix gather of P
+      Ps.resize((size_t)nbe * nbe);
+      for (int j = 0; j < nbe; ++j)
+        for (int i = 0; i < nbe; ++i) Ps[(size_t)j * nbe + i] = P[(size_t)bf[j] * nbf + bf[i]];
+      // X = 2 * P_sub * B   (nbe x npts)
+      X.resize(ne);
+      gemm(nbe, npts, nbe, 2.0, Ps.data(), nbe, f.data(), nbe, false, X.data(), nbe);
+      rho.resize(npts);
+      gxv.assign(npts, 0.);
+      gyv.assign(npts, 0.);
+      gzv.assign(npts, 0.);
+      double exc_t = 0., nel_t = 0.;
+      std::vector<double> a(npts), bx(npts), by(npts), bz(npts);
+      for (int p = 0; p < npts; ++p) {
+        const double* xp = X.data() + (size_t)p * nbe;
+        const double* fp = f.data() + (size_t)p * nbe;
+        double r = 0., dx = 0., dy = 0., dz = 0.;
+        for (int i = 0; i < nbe; ++i) r += fp[i] * xp[i];
+        if (gga) {
+          for (int i = 0; i < nbe; ++i) {
+            dx += fx[(size_t)p * nbe + i] * xp[i];
+            dy += fy[(size_t)p * nbe + i] * xp[i];
+            dz += fz[(size_t)p * nbe + i] * xp[i];
+          }
+          dx *= 2.;
+          dy *= 2.;
+          dz *= 2.;
+        }
+        const double sigma = dx * dx + dy * dy + dz * dz;
+        double eps, vr, vs;
+        eval_functional(func, r, sigma, eps, vr, vs);
+        const double w = tw[p];
+        exc_t += (eps * w) * r;
+        nel_t += w * r;
+        a[p] = 0.5 * vr * w;
+        const double gf = 2. * vs * w;
+        bx[p] = gf * dx;
+        by[p] = gf * dy;
+        bz[p] = gf * dz;
+      }
+      EXC += exc_t;
+      NEL += nel_t;
+      if (!VXC) continue;
+      // Z = 0.5 vrho w B + 2 vsigma w (grad rho . grad B)
+      Zm.resize(ne);
+      for (int p = 0; p < npts; ++p)
+        for (int i = 0; i < nbe; ++i) {
+          const size_t o = (size_t)p * nbe + i;
+          double z = a[p] * f[o];
+          if (gga) z += bx[p] * fx[o] + by[p] * fy[o] + bz[p] * fz[o];
+          Zm[o] = z;
+        }
+      // V = B Z^T + Z B^T (nbe x nbe), lower triangle scattered atomically
+      V.resize((size_t)nbe * nbe);
+      gemm(nbe, nbe, npts, 1.0, f.data(), nbe, Zm.data(), nbe, true, V.data(), nbe);
+      for (int j = 0; j < nbe; ++j)
+        for (int i = j; i < nbe; ++i) {
+          const double v = V[(size_t)j * nbe + i] + V[(size_t)i * nbe + j];
+          const int gi = bf[i], gj = bf[j];
+          // lower triangle of the global matrix
+          const int r_ = std::max(gi, gj), c_ = std::min(gi, gj);
+#pragma omp atomic
+          VXC[(size_t)c_ * nbf + r_] += v;
+        }
+    }
+  }
+  if (VXC)
+    for (int j = 0; j < nbf; ++j)
+      for (int i = j + 1; i < nbf; ++i) VXC[(size_t)i * nbf + j] = VXC[(size_t)j * nbf + i];
+  exc_nel[0] = EXC;
+  exc_nel[1] = NEL;
+}
+
+}  // extern "C"
