@@ -26,18 +26,40 @@ __all__ = [
     "DeviceRuntimeEnvironment", "LoadBalancer", "LoadBalancerFactory",
     "MolecularWeightsSettings", "MolecularWeights", "MolecularWeightsFactory",
     "functional_type", "XCIntegrator", "XCIntegratorFactory", "lib", "device_count",
-    "ssf_weights", "collocation",
+    "ssf_weights", "collocation", "set_device", "measure_fp64_peak",
 ]
 
-_L = load_library()
+class _LazyLibrary:
+    """Loads the native library on first use (so the build module can be imported
+    before the library exists); any missing library or symbol raises then."""
+
+    _cdll = None
+
+    def __getattr__(self, name):
+        if _LazyLibrary._cdll is None:
+            _LazyLibrary._cdll = load_library()
+        return getattr(_LazyLibrary._cdll, name)
+
+
+_L = _LazyLibrary()
 
 
 def lib():
-    return _L
+    _L.gauxc_gb300_version  # force the load
+    return _LazyLibrary._cdll
 
 
 def device_count():
     return int(_L.gauxc_gb300_device_count())
+
+
+def set_device(dev):
+    _call(_L.gauxc_gb300_set_device, int(dev))
+
+
+def measure_fp64_peak():
+    """Measured FP64 FMA throughput of the current GPU, TFLOP/s."""
+    return float(_call(_L.gauxc_gb300_measure_fp64_peak))
 
 
 class ExecutionSpace(enum.IntEnum):
@@ -371,6 +393,15 @@ class XCIntegrator(_Handle):
         out = (ctypes.c_double * 4)()
         _call(_L.gauxc_gb300_integrator_timings, self._h, out, 4)
         return dict(zip(["h2d_ms", "compute_ms", "d2h_ms", "wall_ms"], list(out)))
+
+    def set_profiling(self, on=True):
+        _call(_L.gauxc_gb300_integrator_set_profiling, self._h, ctypes.c_bool(on))
+
+    def kernel_times(self):
+        out = (ctypes.c_double * 10)()
+        _call(_L.gauxc_gb300_integrator_kernel_times, self._h, out, 10)
+        names = ["collocation", "density", "zmat", "vxc", "other"]
+        return {n: dict(ms=out[2 * i], launches=int(out[2 * i + 1])) for i, n in enumerate(names)}
 
     def plan_stats(self):
         out = (ctypes.c_double * 9)()

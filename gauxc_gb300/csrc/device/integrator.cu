@@ -95,6 +95,7 @@ class DeviceIntegrator {
     build(lb);
   }
   ~DeviceIntegrator() {
+    for (auto& e : pev_) cudaEventDestroy(e);
     for (auto& e : ev_) cudaEventDestroy(e);
     if (stream_) cudaStreamDestroy(stream_);
   }
@@ -102,6 +103,10 @@ class DeviceIntegrator {
   uint64_t generation = 0;
   PlanStats stats;
   std::map<std::string, double> timings;
+  bool profiling = false;
+  // per kernel class: accumulated ms and launch count of the last call
+  double kclass_ms[5] = {0, 0, 0, 0, 0};
+  int64_t kclass_n[5] = {0, 0, 0, 0, 0};
 
   void eval(const double* P, int64_t ldp, double* VXC, int64_t ldvxc, double* EXC, double* NEL,
             bool den_only);
@@ -133,6 +138,27 @@ class DeviceIntegrator {
   double* V_ = nullptr;
   double* out_ = nullptr;
   MixedWorkspace mixed_{};
+  std::vector<cudaEvent_t> pev_;
+  std::vector<int> pev_class_;
+  size_t pev_used_ = 0;
+  // bracket one launch of kernel class k with events when profiling
+  template <typename F>
+  int64_t timed(int k, F&& launch) {
+    if (!profiling) return launch();
+    while (pev_.size() < pev_used_ + 2) {
+      cudaEvent_t e;
+      GB300_CUDA(cudaEventCreate(&e));
+      pev_.push_back(e);
+      pev_class_.push_back(0);
+    }
+    GB300_CUDA(cudaEventRecord(pev_[pev_used_], stream_));
+    const int64_t n = launch();
+    GB300_CUDA(cudaEventRecord(pev_[pev_used_ + 1], stream_));
+    pev_class_[pev_used_] = k;
+    pev_class_[pev_used_ + 1] = (int)n;
+    pev_used_ += 2;
+    return n;
+  }
 };
 
 void DeviceIntegrator::build(const LoadBalancer& lb) {
@@ -306,38 +332,47 @@ void DeviceIntegrator::eval(const double* P, int64_t ldp, double* VXC, int64_t l
   const bool do_vxc = (VXC != nullptr) && !den_only;
   if (do_vxc) GB300_CUDA(cudaMemsetAsync(A_, 0, (size_t)nbf_ * nbf_ * sizeof(double), s));
   int64_t launches = 0;
+  pev_used_ = 0;
   for (const Batch& b : batches_) {
     const int nt = b.t_end - b.t_begin;
-    launch_collocation(sh_, tk_, coll_items_ + b.coll_begin, b.coll_end - b.coll_begin, scr_, gga_, s);
-    ++launches;
-    if (prec_ == Precision::Mixed) {
-      launches += launch_density_mixed(mixed_, tk_, b.t_begin, b.t_end, dens_items_ + b.dens_begin,
-                                       b.dens_end - b.dens_begin, scr_, P_, nbf_, func_, zcoef_,
-                                       partials_ + b.dens_begin, s);
-    } else {
+    launches += timed(0, [&] {
+      launch_collocation(sh_, tk_, coll_items_ + b.coll_begin, b.coll_end - b.coll_begin, scr_,
+                         gga_, s);
+      return (int64_t)1;
+    });
+    launches += timed(1, [&]() -> int64_t {
+      if (prec_ == Precision::Mixed)
+        return launch_density_mixed(mixed_, tk_, b.t_begin, b.t_end, dens_items_ + b.dens_begin,
+                                    b.dens_end - b.dens_begin, scr_, P_, nbf_, func_, zcoef_,
+                                    partials_ + b.dens_begin, s);
       launch_density_fp64(tk_, dens_items_ + b.dens_begin, b.dens_end - b.dens_begin, scr_, P_,
                           nbf_, func_, zcoef_, partials_ + b.dens_begin, s);
-      ++launches;
-    }
+      return 1;
+    });
     if (do_vxc) {
-      launch_zmat(tk_, b.t_begin, nt, zcoef_, scr_, gga_, s);
-      ++launches;
-      if (prec_ == Precision::Mixed) {
-        launches += launch_vxc_mixed(mixed_, tk_, b.t_begin, b.t_end, vxc_items_ + b.vxc_begin,
-                                     b.vxc_end - b.vxc_begin, scr_, A_, nbf_, gga_, s);
-      } else {
+      launches += timed(2, [&] {
+        launch_zmat(tk_, b.t_begin, nt, zcoef_, scr_, gga_, s);
+        return (int64_t)1;
+      });
+      launches += timed(3, [&]() -> int64_t {
+        if (prec_ == Precision::Mixed)
+          return launch_vxc_mixed(mixed_, tk_, b.t_begin, b.t_end, vxc_items_ + b.vxc_begin,
+                                  b.vxc_end - b.vxc_begin, scr_, A_, nbf_, gga_, s);
         launch_vxc_fp64(tk_, vxc_items_ + b.vxc_begin, b.vxc_end - b.vxc_begin, scr_, A_, nbf_,
                         gga_, s);
-        ++launches;
-      }
+        return 1;
+      });
     }
   }
-  if (do_vxc) {
-    launch_symmetrize(A_, nbf_, V_, nbf_, s);
-    ++launches;
-  }
-  launch_reduce_partials(partials_, ndens_, out_, s);
-  ++launches;
+  if (do_vxc)
+    launches += timed(4, [&] {
+      launch_symmetrize(A_, nbf_, V_, nbf_, s);
+      return (int64_t)1;
+    });
+  launches += timed(4, [&] {
+    launch_reduce_partials(partials_, ndens_, out_, s);
+    return (int64_t)1;
+  });
   GB300_CUDA(cudaEventRecord(ev_[2], s));
   if (do_vxc)
     GB300_CUDA(cudaMemcpy2DAsync(VXC, (size_t)ldvxc * sizeof(double), V_, row, row, nbf_,
@@ -359,6 +394,16 @@ void DeviceIntegrator::eval(const double* P, int64_t ldp, double* VXC, int64_t l
   timings["wall_ms"] = std::chrono::duration<double, std::milli>(t_host1 - t_host0).count();
   stats.gpu_launches = launches;
   timings["gpu_launches"] = (double)launches;
+  for (int k = 0; k < 5; ++k) {
+    kclass_ms[k] = 0.;
+    kclass_n[k] = 0;
+  }
+  for (size_t i = 0; i < pev_used_; i += 2) {
+    float ms = 0.f;
+    GB300_CUDA(cudaEventElapsedTime(&ms, pev_[i], pev_[i + 1]));
+    kclass_ms[pev_class_[i]] += ms;
+    kclass_n[pev_class_[i]] += pev_class_[i + 1];
+  }
 }
 
 // ---------------------------------------------------------------- API glue
@@ -372,6 +417,7 @@ void ensure_plan(XCIntegratorHandle& h) {
     if (h.rt && h.rt->user_mem) h.rt->user_used = 0;
     h.dev = std::make_shared<DeviceIntegrator>(*h.lb, *h.func, h.prec, *h.rt);
   }
+  h.dev->profiling = h.profiling;
 }
 void check_dims(const XCIntegratorHandle& h, int64_t m, int64_t n, int64_t ldp) {
   const int64_t nbf = h.lb->basis->nbf;
@@ -408,6 +454,21 @@ void integrator_integrate_den(XCIntegratorHandle& h, int64_t m, int64_t n, const
 
 std::map<std::string, double> integrator_timings(const XCIntegratorHandle& h) {
   return h.dev ? h.dev->timings : std::map<std::string, double>{};
+}
+
+void integrator_set_profiling(XCIntegratorHandle& h, bool on) {
+  h.profiling = on;
+  if (h.dev) h.dev->profiling = on;
+}
+
+std::vector<double> integrator_kernel_times(const XCIntegratorHandle& h) {
+  std::vector<double> v(10, 0.);
+  if (!h.dev) return v;
+  for (int k = 0; k < 5; ++k) {
+    v[2 * k] = h.dev->kclass_ms[k];
+    v[2 * k + 1] = (double)h.dev->kclass_n[k];
+  }
+  return v;
 }
 
 PlanStats integrator_plan_stats(XCIntegratorHandle& h) {

@@ -699,6 +699,35 @@ int gauxc_gb300_integrator_plan_stats(GauXCStatus* status, const GauXCIntegrator
   return n;
 }
 
+void gauxc_gb300_integrator_set_profiling(GauXCStatus* status, const GauXCIntegrator integrator,
+                                          bool on) {
+  status_init(status);
+  if (!check(status, integrator, GauXC_Type_Integrator, "Integrator")) return;
+  integrator_set_profiling(*deref<XCIntegratorHandle>(integrator.ptr), on);
+}
+
+int gauxc_gb300_integrator_kernel_times(GauXCStatus* status, const GauXCIntegrator integrator,
+                                        double* out, int nmax) {
+  status_init(status);
+  if (!check(status, integrator, GauXC_Type_Integrator, "Integrator")) return 0;
+  auto v = integrator_kernel_times(*deref<XCIntegratorHandle>(integrator.ptr));
+  int n = 0;
+  for (; n < (int)v.size() && n < nmax; ++n) out[n] = v[n];
+  return n;
+}
+
+double gauxc_gb300_measure_fp64_peak(GauXCStatus* status) {
+  status_init(status);
+  double r = 0.;
+  guarded(status, [&] { r = measure_fp64_peak(); });
+  return r;
+}
+
+void gauxc_gb300_set_device(GauXCStatus* status, int device) {
+  status_init(status);
+  guarded(status, [&] { set_device(device); });
+}
+
 void gauxc_gb300_ssf_weights(GauXCStatus* status, int64_t npts, int32_t natoms,
                              const double* points, const int32_t* iparent,
                              const double* dist_nearest, const double* coords, double* weights) {

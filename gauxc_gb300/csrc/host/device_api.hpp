@@ -40,6 +40,7 @@ struct XCIntegratorHandle {
   Precision prec = Precision::FP64;
   std::shared_ptr<DeviceIntegrator> dev;
   double last_exc = 0., last_nel = 0.;
+  bool profiling = false;
 };
 
 // eval_exc_vxc for RKS; VXC may be null (EXC only).  Throws gb300::error.
@@ -49,6 +50,14 @@ void integrator_integrate_den(XCIntegratorHandle& h, int64_t m, int64_t n, const
                               int64_t ldp, double* NEL);
 std::map<std::string, double> integrator_timings(const XCIntegratorHandle& h);
 PlanStats integrator_plan_stats(XCIntegratorHandle& h);
+// Per-kernel-class CUDA-event timing of every launch (collocation, density,
+// zmat, vxc, other): {ms, launches} pairs of the last call.
+void integrator_set_profiling(XCIntegratorHandle& h, bool on);
+std::vector<double> integrator_kernel_times(const XCIntegratorHandle& h);
+
+// FP64 FMA throughput probe (TFLOP/s) on the current device.
+double measure_fp64_peak();
+void set_device(int dev);
 
 // SSF weights on the device for every task of the load balancer.
 void molecular_weights_ssf_device(LoadBalancer& lb, RuntimeEnv& rt);

@@ -254,6 +254,19 @@ int gauxc_gb300_integrator_timings(GauXCStatus* status, const GauXCIntegrator in
 int gauxc_gb300_integrator_plan_stats(GauXCStatus* status, const GauXCIntegrator integrator,
                                       double* out, int nmax);
 
+/* Per-kernel-class CUDA-event timing of each launch of the following calls
+   (adds two events per launch on the integrator's stream). */
+void gauxc_gb300_integrator_set_profiling(GauXCStatus* status, const GauXCIntegrator integrator,
+                                          bool on);
+/* {collocation ms, launches, density ms, launches, zmat ms, launches, vxc ms,
+   launches, other ms, launches} of the last call; returns the count written. */
+int gauxc_gb300_integrator_kernel_times(GauXCStatus* status, const GauXCIntegrator integrator,
+                                        double* out, int nmax);
+/* Measured FP64 FMA throughput of the current device in TFLOP/s (about 50 ms probe). */
+double gauxc_gb300_measure_fp64_peak(GauXCStatus* status);
+/* cudaSetDevice for the calling thread (one process per GPU). */
+void gauxc_gb300_set_device(GauXCStatus* status, int device);
+
 /* Stage entry points (host arrays, computed on the device).
    SSF weights, reference kernel cuda_ssf_1d.cu:24-144 (partition_weights_ssf_1d). */
 void gauxc_gb300_ssf_weights(GauXCStatus* status, int64_t npts, int32_t natoms,
