@@ -34,6 +34,7 @@ WORKLOADS = {
     1: "32 waters (10 A cube), PBE, MK 99x590 Treutler, 1920 bf, nocc 160",
     2: "96 waters (14 A cube), PBE, MK 75x302 Treutler, 5760 bf, nocc 480",
     4: "256 waters (20 A cube), PBE, MK 75x302 Treutler, tol 1e-12, 15360 bf, nocc 1280",
+    5: "profiling case: 4 waters (6 A cube), PBE, MK 99x590 Treutler, 240 bf",
 }
 
 

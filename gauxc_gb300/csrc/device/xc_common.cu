@@ -14,18 +14,21 @@ namespace {
 
 __global__ void symmetrize_kernel(const double* __restrict__ A, int n, double* __restrict__ V,
                                   int64_t ld) {
-  __shared__ double tile[32][33];
-  const int bi = blockIdx.x * 32, bj = blockIdx.y * 32;
-  // load A(bj + ty, bi + tx) transposed into tile
-  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
-    const int row = bi + threadIdx.x, col = bj + r;
-    if (row < n && col < n) tile[r][threadIdx.x] = A[(int64_t)row * n + col];
+  // output block: rows [r0, r0+32), columns [c0, c0+32) of V (column-major)
+  __shared__ double T[32][33];
+  const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+  const int tx = threadIdx.x;
+  // T[y][x] = A(c0 + x, r0 + y): coalesced along x
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const int row = c0 + tx, col = r0 + y;
+    if (row < n && col < n) T[y][tx] = A[(int64_t)col * n + row];
   }
   __syncthreads();
-  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
-    const int row = bj + threadIdx.x, col = bi + r;  // element (row, col) of V, col-major
+  // V(r0 + tx, c0 + y) = A(r0 + tx, c0 + y) + A(c0 + y, r0 + tx)
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const int row = r0 + tx, col = c0 + y;
     if (row < n && col < n)
-      V[(int64_t)col * ld + row] = A[(int64_t)col * n + row] + tile[threadIdx.x][r];
+      V[(int64_t)col * ld + row] = A[(int64_t)col * n + row] + T[tx][y];
   }
 }
 

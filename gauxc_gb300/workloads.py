@@ -8,6 +8,8 @@ The five workloads (index 0-4) are:
      MK 75 x 302 Treutler, batch sizes 128-1024, nocc = 5 n_water
   4  256 waters in a 20 A cube, PBE, MK 75 x 302 Treutler, shell tol 1e-12,
      15360 bf, nocc 1280
+  5  profiling case: 4 waters in a 6 A cube, PBE, MK 99 x 590 Treutler, 240 bf
+     (same kernels as 1 with a few GB of device memory)
 Water geometry: O at (0,0,0) A, H at (+-0.757, 0.587, 0) A; clusters apply
 uniform random rotations (Shoemake quaternions) and uniform random centres
 in the cube, rejecting placements with an O-O distance below 2.6 A.
@@ -22,7 +24,7 @@ BOHR_PER_ANG = 1.0 / 0.529177210903
 WATER_ANG = np.array([[0.0, 0.0, 0.0], [0.757, 0.587, 0.0], [-0.757, 0.587, 0.0]])
 WATER_Z = [8, 1, 1]
 
-SEEDS = {0: 1000, 1: 1001, 2: 1002, 3: 1003, 4: 1004}
+SEEDS = {0: 1000, 1: 1001, 2: 1002, 3: 1003, 4: 1004, 5: 1005}
 
 
 def _rotation(u):
@@ -95,6 +97,8 @@ def config(idx):
             specs.append((n, cube, "SVWN5" if i % 2 == 0 else "PBE", "Treutler", "FineGrid", bs, 1e-10))
     elif idx == 4:
         specs = [(256, 20.0, "PBE", "Treutler", "FineGrid", 512, 1e-12)]
+    elif idx == 5:
+        specs = [(4, 6.0, "PBE", "Treutler", "UltraFineGrid", 512, 1e-10)]
     else:
         raise ValueError(idx)
     systems = []
