@@ -263,7 +263,7 @@ def main():
     nbf = s["nbf"]
     stats = integ.plan_stats()
 
-    for _ in range(max(args.warmup, 3) if args.warmup > 0 else 0):
+    for _ in range(args.warmup):
         eval_into(integ, P, V)
     fp64_peak = g.measure_fp64_peak()
     integ.set_profiling(True)
