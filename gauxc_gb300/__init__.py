@@ -57,6 +57,11 @@ def set_device(dev):
     _call(_L.gauxc_gb300_set_device, int(dev))
 
 
+def tensor_core_selftest(n=256, k=512):
+    """Worst relative error of the tensor-core emulated-FP64 GEMM on random data."""
+    return float(_call(_L.gauxc_gb300_tensor_core_selftest, int(n), int(k)))
+
+
 def measure_fp64_peak():
     """Measured FP64 FMA throughput of the current GPU, TFLOP/s."""
     return float(_call(_L.gauxc_gb300_measure_fp64_peak))

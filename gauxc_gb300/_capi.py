@@ -116,6 +116,7 @@ PROTOTYPES = {
     "gauxc_gb300_integrator_kernel_times": (I, [S, GauXCIntegrator, P(dbl), I]),
     "gauxc_gb300_measure_fp64_peak": (dbl, [S]),
     "gauxc_gb300_set_device": (None, [S, I]),
+    "gauxc_gb300_tensor_core_selftest": (dbl, [S, I, I]),
     "gauxc_gb300_ssf_weights": (None, [S, i64, i32, P(dbl), P(i32), P(dbl), P(dbl), P(dbl)]),
     "gauxc_gb300_collocation": (None, [S, GauXCBasisSet, i64, P(dbl), i32, P(i32), P(dbl),
                                        P(dbl), P(dbl), P(dbl)]),

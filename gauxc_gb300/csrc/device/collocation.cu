@@ -12,6 +12,7 @@
 // One thread owns one point and walks the task's shell list, so every store
 // of a warp covers 32 consecutive points of one column.
 #include "device_common.cuh"
+#include "xc_mixed.cuh"
 #include "collocation_angular.inc"
 
 namespace gb300 {
@@ -61,8 +62,11 @@ __device__ __forceinline__ void eval_shell(int l, int pure, double x, double y, 
   }
 }
 
-template <bool GRAD>
-__global__ void __launch_bounds__(128) collocation_kernel(ShellsDev sh, TasksDev tk,
+// With MASK, a block of merged tasks is evaluated on its union shell list and
+// a shell outside the point's own task list contributes exact zeros, so the
+// merged block reproduces the per-task screening of the reference.
+template <bool GRAD, bool MASK>
+__global__ void __launch_bounds__(128) collocation_kernel(ShellsDev sh, TasksDev tk, PBMaskDev mk,
                                                           const int2* __restrict__ items,
                                                           double* __restrict__ scr) {
   const int2 it = items[blockIdx.x];
@@ -80,9 +84,24 @@ __global__ void __launch_bounds__(128) collocation_kernel(ShellsDev sh, TasksDev
   double* fz = fy + blk;
   const int64_t s0 = tk.sh_off[t];
   const int ns = tk.nsh[t];
+  const uint8_t* active = nullptr;
+  if (MASK) active = mk.mask + mk.mask_off[t] + (int64_t)mk.member[g] * ns;
   for (int i = 0; i < ns; ++i) {
     const int s = tk.sh_list[s0 + i];
     const int col = tk.sh_col[s0 + i];
+    if (MASK && !active[i]) {
+      const int sz = sh.pure[s] ? 2 * sh.l[s] + 1 : (sh.l[s] + 1) * (sh.l[s] + 2) / 2;
+      for (int m = 0; m < sz; ++m) {
+        const int64_t o = (int64_t)(col + m) * ld + p;
+        f[o] = 0.;
+        if (GRAD) {
+          fx[o] = 0.;
+          fy[o] = 0.;
+          fz[o] = 0.;
+        }
+      }
+      continue;
+    }
     const double dx = px - sh.origin[3 * s + 0];
     const double dy = py - sh.origin[3 * s + 1];
     const double dz = pz - sh.origin[3 * s + 2];
@@ -114,10 +133,22 @@ __global__ void __launch_bounds__(128) collocation_kernel(ShellsDev sh, TasksDev
 void launch_collocation(const ShellsDev& sh, const TasksDev& tk, const int2* items, int nitems,
                         double* scr, bool grad, cudaStream_t s) {
   if (nitems == 0) return;
+  const PBMaskDev none{};
   if (grad)
-    collocation_kernel<true><<<nitems, 128, 0, s>>>(sh, tk, items, scr);
+    collocation_kernel<true, false><<<nitems, 128, 0, s>>>(sh, tk, none, items, scr);
   else
-    collocation_kernel<false><<<nitems, 128, 0, s>>>(sh, tk, items, scr);
+    collocation_kernel<false, false><<<nitems, 128, 0, s>>>(sh, tk, none, items, scr);
+  GB300_CUDA(cudaGetLastError());
+}
+
+void launch_collocation_masked(const ShellsDev& sh, const TasksDev& tk, const PBMaskDev& mk,
+                               const int2* items, int nitems, double* scr, bool grad,
+                               cudaStream_t s) {
+  if (nitems == 0) return;
+  if (grad)
+    collocation_kernel<true, true><<<nitems, 128, 0, s>>>(sh, tk, mk, items, scr);
+  else
+    collocation_kernel<false, true><<<nitems, 128, 0, s>>>(sh, tk, mk, items, scr);
   GB300_CUDA(cudaGetLastError());
 }
 

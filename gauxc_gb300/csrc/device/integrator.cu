@@ -18,6 +18,7 @@
 #include <cmath>
 #include <cstring>
 #include <numeric>
+#include <iterator>
 
 #include "../host/device_api.hpp"
 #include "device_common.cuh"
@@ -82,6 +83,17 @@ struct Batch {
   int vxc_begin, vxc_end;
 };
 
+// One batch of point blocks of the mixed path.
+struct MBatch {
+  int b0, b1;                // point blocks
+  int coll_begin, coll_end;  // collocation items
+  int x_begin, x_end;        // density GEMM tiles
+  int v_begin, v_end;        // VXC GEMM tiles
+  int64_t g0, g1;            // point range
+  int max_nu_pad;
+  int partial_base;
+};
+
 }  // namespace
 
 class DeviceIntegrator {
@@ -113,6 +125,8 @@ class DeviceIntegrator {
 
  private:
   void build(const LoadBalancer& lb);
+  void build_mixed(const LoadBalancer& lb);
+  int64_t eval_mixed_batches(bool do_vxc);
 
   XCFunctionalDesc func_;
   Precision prec_;
@@ -137,7 +151,16 @@ class DeviceIntegrator {
   double* A_ = nullptr;
   double* V_ = nullptr;
   double* out_ = nullptr;
-  MixedWorkspace mixed_{};
+  // mixed path (point blocks)
+  PBMaskDev mk_{};
+  MixedPBDev mp_{};
+  std::vector<MBatch> mbatches_;
+  OzItem* x_items_ = nullptr;
+  OzItem* v_items_ = nullptr;
+  double* f64_ = nullptr;
+  __nv_bfloat16* dig_ = nullptr;
+  double* rho4_ = nullptr;
+  int* err_ = nullptr;
   std::vector<cudaEvent_t> pev_;
   std::vector<int> pev_class_;
   size_t pev_used_ = 0;
@@ -189,6 +212,19 @@ void DeviceIntegrator::build(const LoadBalancer& lb) {
     sh_.origin = arena_.upload(o, s);
     sh_.l = arena_.upload(l, s);
     sh_.pure = arena_.upload(pure, s);
+  }
+
+  P_ = arena_.alloc<double>((size_t)nbf_ * nbf_);
+  A_ = arena_.alloc<double>((size_t)nbf_ * nbf_);
+  V_ = arena_.alloc<double>((size_t)nbf_ * nbf_);
+  out_ = arena_.alloc<double>(2);
+  err_ = arena_.alloc<int>(1);
+  GB300_CUDA(cudaMemsetAsync(err_, 0, sizeof(int), s));
+  if (prec_ == Precision::Mixed) {
+    build_mixed(lb);
+    GB300_CUDA(cudaStreamSynchronize(s));
+    generation = lb.generation;
+    return;
   }
 
   // ---- task order: npts * nbe descending (stable)
@@ -310,14 +346,257 @@ void DeviceIntegrator::build(const LoadBalancer& lb) {
   scr_ = arena_.alloc<double>((size_t)(max_used / 8.) + 1);
   zcoef_ = arena_.alloc<double4>(std::max<int64_t>(pts, 1));
   partials_ = arena_.alloc<double2>(std::max(ndens_, 1));
-  P_ = arena_.alloc<double>((size_t)nbf_ * nbf_);
-  A_ = arena_.alloc<double>((size_t)nbf_ * nbf_);
-  V_ = arena_.alloc<double>((size_t)nbf_ * nbf_);
-  out_ = arena_.alloc<double>(2);
-  if (prec_ == Precision::Mixed) mixed_ = mixed_workspace_create(nt, npts_pad, nbe_pad, scr_off,
-                                                                 [&](size_t b) { return arena_.alloc<char>(b); });
   GB300_CUDA(cudaStreamSynchronize(s));
   generation = lb.generation;
+}
+
+// Point blocks for the tensor-core path: consecutive tasks of one parent atom
+// (the load balancer orders them by shell list) are merged while the block
+// holds at most kPBMaxPts points and its union basis stays within 25 % of its
+// largest member's; a task larger than kPBMaxPts points is split.  The union
+// basis is padded to kMTile rows, the points to kNTile columns.
+void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
+  const BasisSet& bs = *lb.basis;
+  cudaStream_t s = stream_;
+  const auto& tasks = lb.tasks;
+  struct Seg {
+    int task, p0, p1;
+  };
+  struct PB {
+    int iparent;
+    std::vector<Seg> segs;
+    std::vector<int> shells;  // sorted union
+    int nu = 0, npts = 0;
+  };
+  auto nbe_of = [&](const std::vector<int>& sl) {
+    int n = 0;
+    for (int x : sl) n += bs.shells[x].size();
+    return n;
+  };
+  std::vector<PB> pbs;
+  for (int t = 0; t < (int)tasks.size(); ++t) {
+    const XCTask& tt = tasks[t];
+    for (int p0 = 0; p0 < tt.npts; p0 += kPBMaxPts) {
+      const int p1 = std::min(tt.npts, p0 + kPBMaxPts);
+      bool merged = false;
+      if (!pbs.empty() && pbs.back().iparent == tt.iParent &&
+          pbs.back().npts + (p1 - p0) <= kPBMaxPts) {
+        PB& b = pbs.back();
+        std::vector<int> u;
+        std::set_union(b.shells.begin(), b.shells.end(), tt.shell_list.begin(),
+                       tt.shell_list.end(), std::back_inserter(u));
+        const int nu = nbe_of(u);
+        if (nu * 4 <= std::max(b.nu, tt.nbe) * 5) {
+          b.shells.swap(u);
+          b.nu = nu;
+          b.npts += p1 - p0;
+          b.segs.push_back({t, p0, p1});
+          merged = true;
+        }
+      }
+      if (!merged) {
+        PB b;
+        b.iparent = tt.iParent;
+        b.segs.push_back({t, p0, p1});
+        b.shells.assign(tt.shell_list.begin(), tt.shell_list.end());
+        b.nu = tt.nbe;
+        b.npts = p1 - p0;
+        pbs.push_back(std::move(b));
+      }
+    }
+  }
+  // largest blocks first (load balance inside each launch)
+  std::vector<int> order(pbs.size());
+  std::iota(order.begin(), order.end(), 0);
+  auto cost = [&](int i) {
+    const double np = (double)round_up(pbs[i].npts, kNTile), nu = (double)round_up(pbs[i].nu, kMTile);
+    return np * nu * nu;
+  };
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost(a) > cost(b); });
+
+  const int npb = (int)pbs.size();
+  std::vector<int64_t> pt_off(npb), bf_off(npb), sh_off(npb), f64_off(npb), dig_off(npb),
+      mask_off(npb);
+  std::vector<int> npts_pad(npb), nu(npb), nu_pad(npb), nsh(npb), bf_list, sh_list, sh_col,
+      member;
+  std::vector<uint8_t> mask;
+  std::vector<double> X, Y, Z, W;
+  stats = PlanStats{};
+  int64_t pts = 0;
+  for (int i = 0; i < npb; ++i) {
+    const PB& b = pbs[order[i]];
+    pt_off[i] = pts;
+    npts_pad[i] = (int)round_up(b.npts, kNTile);
+    nu[i] = b.nu;
+    nu_pad[i] = (int)round_up(b.nu, kMTile);
+    nsh[i] = (int)b.shells.size();
+    sh_off[i] = (int64_t)sh_list.size();
+    bf_off[i] = (int64_t)bf_list.size();
+    int col = 0;
+    for (int x : b.shells) {
+      sh_list.push_back(x);
+      sh_col.push_back(col);
+      for (int k = 0; k < bs.shells[x].size(); ++k) bf_list.push_back(bs.shell_offs[x] + k);
+      col += bs.shells[x].size();
+    }
+    for (int k = col; k < nu_pad[i]; ++k) bf_list.push_back(-1);
+    mask_off[i] = (int64_t)mask.size();
+    for (size_t m = 0; m < b.segs.size(); ++m) {
+      const XCTask& tt = tasks[b.segs[m].task];
+      for (int x : b.shells)
+        mask.push_back(std::binary_search(tt.shell_list.begin(), tt.shell_list.end(), x) ? 1 : 0);
+    }
+    int np_real = 0;
+    for (size_t m = 0; m < b.segs.size(); ++m) {
+      const Seg& sg = b.segs[m];
+      const XCTask& tt = tasks[sg.task];
+      for (int p = sg.p0; p < sg.p1; ++p) {
+        X.push_back(tt.points[3 * p]);
+        Y.push_back(tt.points[3 * p + 1]);
+        Z.push_back(tt.points[3 * p + 2]);
+        W.push_back(tt.weights[p]);
+        member.push_back((int)m);
+        ++np_real;
+      }
+    }
+    for (int p = np_real; p < npts_pad[i]; ++p) {
+      X.push_back(X[pts]);
+      Y.push_back(Y[pts]);
+      Z.push_back(Z[pts]);
+      W.push_back(0.);
+      member.push_back(0);
+    }
+    pts += npts_pad[i];
+    stats.npts += b.npts;
+    stats.sum_pad_npts_nbe2 += (double)npts_pad[i] * nu_pad[i] * nu_pad[i];
+  }
+  for (const auto& t : tasks) {
+    stats.sum_npts_nbe += (double)t.npts * t.nbe;
+    stats.sum_npts_nbe2 += (double)t.npts * t.nbe * t.nbe;
+  }
+  stats.ntasks = (int64_t)tasks.size();
+  stats.npts_pad = pts;
+
+  // ---- batches under the workspace budget
+  size_t free_b = 0, total_b = 0;
+  GB300_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  const double static_bytes = pts * (3 * 8. + 8. + 32. + 32. + 4.) + bf_list.size() * 4. +
+                              mask.size() + 64e6;
+  double budget = rt_->user_mem ? (double)rt_->user_bytes - rt_->user_used - static_bytes
+                                : rt_->fill_fraction * (double)free_b - static_bytes;
+  if (const char* cap = std::getenv("GAUXC_GB300_SCRATCH_GB")) budget = std::min(budget, atof(cap) * 1e9);
+  budget = std::min(budget, 96e9);
+  std::vector<int2> coll;
+  std::vector<OzItem> xi, vi;
+  double f64_used = 0., dig_used = 0., max_f64 = 0., max_dig = 0.;
+  const int nfb = functional_partial_blocks();
+  MBatch cur{0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  auto close_batch = [&](int i) {
+    cur.b1 = i;
+    cur.coll_end = (int)coll.size();
+    cur.x_end = (int)xi.size();
+    cur.v_end = (int)vi.size();
+    cur.g1 = i > 0 ? pt_off[i - 1] + npts_pad[i - 1] : 0;
+    mbatches_.push_back(cur);
+  };
+  for (int i = 0; i < npb; ++i) {
+    const double nf = (double)mixed_f64_doubles(npts_pad[i], nu_pad[i], gga_) * 8.;
+    const double nd = (double)mixed_dig_elems(npts_pad[i], nu_pad[i]) * 2.;
+    if (nf + nd > budget) throw error("insufficient device memory for one point block");
+    if (f64_used + dig_used + nf + nd > budget && i > cur.b0) {
+      close_batch(i);
+      cur = MBatch{i, i, (int)coll.size(), 0, (int)xi.size(), 0, (int)vi.size(), 0, pt_off[i], 0,
+                   0, (int)mbatches_.size() * nfb};
+      f64_used = dig_used = 0.;
+    }
+    f64_off[i] = (int64_t)(f64_used / 8.);
+    dig_off[i] = (int64_t)(dig_used / 2.);
+    f64_used += std::ceil(nf / 256.) * 256.;
+    dig_used += std::ceil(nd / 256.) * 256.;
+    max_f64 = std::max(max_f64, f64_used);
+    max_dig = std::max(max_dig, dig_used);
+    cur.max_nu_pad = std::max(cur.max_nu_pad, nu_pad[i]);
+    for (int b = 0; b < (npts_pad[i] + 127) / 128; ++b) coll.push_back(make_int2(i, b));
+    for (int m0 = 0; m0 < nu_pad[i]; m0 += kMTile)
+      for (int n0 = 0; n0 < npts_pad[i]; n0 += kNTile)
+        for (int k0 = 0; k0 < nu_pad[i]; k0 += kMaxK)
+          xi.push_back(OzItem{i, m0, n0, k0, std::min(k0 + kMaxK, nu_pad[i])});
+    for (int m0 = 0; m0 < nu_pad[i]; m0 += kMTile)
+      for (int n0 = 0; n0 < nu_pad[i]; n0 += kNTile) vi.push_back(OzItem{i, m0, n0, 0, npts_pad[i]});
+  }
+  if (npb > 0) close_batch(npb);
+  stats.nbatches = (int64_t)mbatches_.size();
+  stats.scratch_bytes = max_f64 + max_dig;
+
+  tk_.ntasks = npb;
+  tk_.pt_off = arena_.upload(pt_off, s);
+  tk_.npts_pad = arena_.upload(npts_pad, s);
+  tk_.nbe = arena_.upload(nu, s);
+  tk_.nbe_pad = arena_.upload(nu_pad, s);
+  tk_.bf_off = arena_.upload(bf_off, s);
+  tk_.bf_list = arena_.upload(bf_list, s);
+  tk_.sh_off = arena_.upload(sh_off, s);
+  tk_.nsh = arena_.upload(nsh, s);
+  tk_.sh_list = arena_.upload(sh_list, s);
+  tk_.sh_col = arena_.upload(sh_col, s);
+  tk_.scr_off = arena_.upload(f64_off, s);
+  tk_.x = arena_.upload(X, s);
+  tk_.y = arena_.upload(Y, s);
+  tk_.z = arena_.upload(Z, s);
+  tk_.w = arena_.upload(W, s);
+  mk_.member = arena_.upload(member, s);
+  mk_.mask_off = arena_.upload(mask_off, s);
+  mk_.mask = arena_.upload(mask, s);
+  mp_.f64_off = tk_.scr_off;
+  mp_.dig_off = arena_.upload(dig_off, s);
+  coll_items_ = arena_.upload(coll, s);
+  x_items_ = arena_.upload(xi, s);
+  v_items_ = arena_.upload(vi, s);
+  f64_ = arena_.alloc<double>((size_t)(max_f64 / 8.) + 32);
+  dig_ = arena_.alloc<__nv_bfloat16>((size_t)(max_dig / 2.) + 128);
+  rho4_ = arena_.alloc<double>((size_t)std::max<int64_t>(pts, 1) * 4);
+  zcoef_ = arena_.alloc<double4>(std::max<int64_t>(pts, 1));
+  ndens_ = (int)mbatches_.size() * nfb;
+  partials_ = arena_.alloc<double2>(std::max(ndens_, 1));
+}
+
+int64_t DeviceIntegrator::eval_mixed_batches(bool do_vxc) {
+  cudaStream_t s = stream_;
+  int64_t launches = 0;
+  for (const MBatch& b : mbatches_) {
+    GB300_CUDA(cudaMemsetAsync(rho4_ + 4 * b.g0, 0, (size_t)(b.g1 - b.g0) * 4 * sizeof(double), s));
+    launches += timed(0, [&] {
+      launch_collocation_masked(sh_, tk_, mk_, coll_items_ + b.coll_begin,
+                                b.coll_end - b.coll_begin, f64_, gga_, s);
+      return (int64_t)1;
+    });
+    launches += timed(4, [&] {
+      launch_point_scales(tk_, mp_, b.b0, b.b1, gga_, f64_, s);
+      launch_phi_digits(tk_, mp_, b.b0, b.b1, gga_, f64_, dig_, s);
+      launch_p_digits(tk_, mp_, b.b0, b.b1, b.max_nu_pad, gga_, P_, nbf_, f64_, dig_, s);
+      return (int64_t)3;
+    });
+    launches += timed(1, [&] {
+      launch_ozaki_x(tk_, mp_, x_items_ + b.x_begin, b.x_end - b.x_begin, f64_, dig_, gga_, rho4_,
+                     err_, s);
+      return (int64_t)1;
+    });
+    launches += timed(4, [&] {
+      launch_functional(b.g0, b.g1, tk_.w, rho4_, func_, zcoef_, partials_ + b.partial_base, s);
+      return (int64_t)1;
+    });
+    if (!do_vxc) continue;
+    launches += timed(2, [&] {
+      launch_z_digits(tk_, mp_, b.b0, b.b1, b.max_nu_pad, gga_, zcoef_, f64_, dig_, s);
+      return (int64_t)1;
+    });
+    launches += timed(3, [&] {
+      launch_ozaki_v(tk_, mp_, v_items_ + b.v_begin, b.v_end - b.v_begin, f64_, dig_, A_, nbf_,
+                     err_, s);
+      return (int64_t)1;
+    });
+  }
+  return launches;
 }
 
 void DeviceIntegrator::eval(const double* P, int64_t ldp, double* VXC, int64_t ldvxc, double* EXC,
@@ -333,6 +612,7 @@ void DeviceIntegrator::eval(const double* P, int64_t ldp, double* VXC, int64_t l
   if (do_vxc) GB300_CUDA(cudaMemsetAsync(A_, 0, (size_t)nbf_ * nbf_ * sizeof(double), s));
   int64_t launches = 0;
   pev_used_ = 0;
+  if (prec_ == Precision::Mixed) launches += eval_mixed_batches(do_vxc);
   for (const Batch& b : batches_) {
     const int nt = b.t_end - b.t_begin;
     launches += timed(0, [&] {
@@ -340,27 +620,20 @@ void DeviceIntegrator::eval(const double* P, int64_t ldp, double* VXC, int64_t l
                          gga_, s);
       return (int64_t)1;
     });
-    launches += timed(1, [&]() -> int64_t {
-      if (prec_ == Precision::Mixed)
-        return launch_density_mixed(mixed_, tk_, b.t_begin, b.t_end, dens_items_ + b.dens_begin,
-                                    b.dens_end - b.dens_begin, scr_, P_, nbf_, func_, zcoef_,
-                                    partials_ + b.dens_begin, s);
+    launches += timed(1, [&] {
       launch_density_fp64(tk_, dens_items_ + b.dens_begin, b.dens_end - b.dens_begin, scr_, P_,
                           nbf_, func_, zcoef_, partials_ + b.dens_begin, s);
-      return 1;
+      return (int64_t)1;
     });
     if (do_vxc) {
       launches += timed(2, [&] {
         launch_zmat(tk_, b.t_begin, nt, zcoef_, scr_, gga_, s);
         return (int64_t)1;
       });
-      launches += timed(3, [&]() -> int64_t {
-        if (prec_ == Precision::Mixed)
-          return launch_vxc_mixed(mixed_, tk_, b.t_begin, b.t_end, vxc_items_ + b.vxc_begin,
-                                  b.vxc_end - b.vxc_begin, scr_, A_, nbf_, gga_, s);
+      launches += timed(3, [&] {
         launch_vxc_fp64(tk_, vxc_items_ + b.vxc_begin, b.vxc_end - b.vxc_begin, scr_, A_, nbf_,
                         gga_, s);
-        return 1;
+        return (int64_t)1;
       });
     }
   }
@@ -379,8 +652,13 @@ void DeviceIntegrator::eval(const double* P, int64_t ldp, double* VXC, int64_t l
                                  cudaMemcpyDeviceToHost, s));
   double en[2];
   GB300_CUDA(cudaMemcpyAsync(en, out_, sizeof(en), cudaMemcpyDeviceToHost, s));
+  int herr = 0;
+  GB300_CUDA(cudaMemcpyAsync(&herr, err_, sizeof(int), cudaMemcpyDeviceToHost, s));
   GB300_CUDA(cudaEventRecord(ev_[3], s));
   GB300_CUDA(cudaStreamSynchronize(s));
+  if (herr)
+    throw error("a tensor-core pipeline wait expired on the device (error code " +
+                std::to_string(herr) + ")");
   auto t_host1 = std::chrono::steady_clock::now();
   if (EXC) *EXC = en[0];
   if (NEL) *NEL = en[1];

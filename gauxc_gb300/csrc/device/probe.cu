@@ -6,6 +6,7 @@
 // a runtime flag that is never set is non-zero, so nothing is eliminated.
 #include "../host/device_api.hpp"
 #include "device_common.cuh"
+#include "xc_mixed.cuh"
 
 namespace gb300 {
 
@@ -57,5 +58,10 @@ double measure_fp64_peak() {
 }
 
 void set_device(int d) { GB300_CUDA(cudaSetDevice(d)); }
+
+double tensor_core_selftest(int n, int k) {
+  if (cuda_device_count() == 0) throw error("no CUDA device available");
+  return ozaki_selftest(n, k);
+}
 
 }  // namespace gb300

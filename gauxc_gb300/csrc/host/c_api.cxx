@@ -723,6 +723,13 @@ double gauxc_gb300_measure_fp64_peak(GauXCStatus* status) {
   return r;
 }
 
+double gauxc_gb300_tensor_core_selftest(GauXCStatus* status, int n, int k) {
+  status_init(status);
+  double r = -1.;
+  guarded(status, [&] { r = tensor_core_selftest(n, k); });
+  return r;
+}
+
 void gauxc_gb300_set_device(GauXCStatus* status, int device) {
   status_init(status);
   guarded(status, [&] { set_device(device); });

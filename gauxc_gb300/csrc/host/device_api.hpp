@@ -57,6 +57,8 @@ std::vector<double> integrator_kernel_times(const XCIntegratorHandle& h);
 
 // FP64 FMA throughput probe (TFLOP/s) on the current device.
 double measure_fp64_peak();
+// Tensor-core emulated-FP64 GEMM self-test: worst relative error.
+double tensor_core_selftest(int n, int k);
 void set_device(int dev);
 
 // SSF weights on the device for every task of the load balancer.
