@@ -28,7 +28,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "EXC+VXC time/SCF iter on 1 GB300"
+METRIC = "EXC+VXC time/SCF iter on 1 GB300: mixed-prec batched vs FP64 GPU at |\u0394EXC|\u22641e-8 Eh"
 WORKLOADS = {
     0: "1 water, SVWN5, MK 75x302 unpruned, 60 bf",
     1: "32 waters (10 A cube), PBE, MK 99x590 Treutler, 1920 bf, nocc 160",
@@ -212,6 +212,8 @@ def main():
     ap.add_argument("--lwd", default="Default")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-check", action="store_true",
+                    help="mixed path: skip the FP64 device pass used for dEXC / dVXC")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     dist = init_dist(ws)
@@ -296,14 +298,14 @@ def main():
     if rank != 0:
         return 0
 
-    # roofline of the dominant kernel class (FP64 FMA pipe for the plain path)
+    # roofline of the dominant kernel class
+    mixed = args.lwd.lower() == "gb300-mixed"
     gga = s["functional"] != "SVWN5"
+    dom = "density" if kt["density"]["ms"] >= kt["vxc"]["ms"] else "vxc"
+    dom_s = kt[dom]["ms"] * 1e-3
     f_x = 2.0 * stats["sum_npts_nbe2"] + 2.0 * stats["sum_npts_nbe"] * (4 if gga else 1)
     f_v = 2.0 * stats["sum_npts_nbe2"]
-    dom = "density" if kt["density"]["ms"] >= kt["vxc"]["ms"] else "vxc"
-    flops = (f_x if dom == "density" else f_v) * args.steps
-    dom_s = kt[dom]["ms"] * 1e-3
-    achieved = flops / dom_s / 1e12
+    f64_flops = (f_x if dom == "density" else f_v) * args.steps
     traffic = None
     tp = os.path.join(ROOT, "profiles", "roofline_traffic.json")
     if os.path.exists(tp):
@@ -311,11 +313,44 @@ def main():
             traffic = json.load(open(tp)).get(f"config{args.config}_{args.lwd}_{dom}")
         except (ValueError, OSError):
             traffic = None
-    roofline = dict(bound="fp64", kernel=dom, achieved=achieved, peak=fp64_peak, unit="TFLOP/s",
-                    frac=achieved / fp64_peak, traffic=traffic,
-                    peak_source="FP64 FMA probe measured in this run (no FP64 figure in the "
-                                "measured-peaks file)",
-                    algorithmic_flops_per_step=flops / args.steps)
+    if mixed:
+        peaks = {}
+        pp = os.path.join(ROOT, "MEASURED_PEAKS.json")
+        if os.path.exists(pp):
+            peaks = json.load(open(pp))
+        peak = peaks.get("bf16_tflops_sustained")
+        src = "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)"
+        if peak is None:
+            peak, src = 1700.0, "fallback sustained bf16 1.7 PFLOP/s (of fallback)"
+        tflops = (stats["tensor_flops_x"] if dom == "density" else stats["tensor_flops_v"]) * args.steps
+        achieved = tflops / dom_s / 1e12
+        roofline = dict(bound="tensor", kernel=f"ozaki_kernel<{'X' if dom == 'density' else 'V'}>",
+                        achieved=achieved, peak=peak, unit="TFLOP/s", frac=achieved / peak,
+                        traffic=traffic, peak_source=src,
+                        algorithmic_flops_per_step=tflops / args.steps,
+                        fp64_equivalent_tflops=f64_flops / dom_s / 1e12)
+    else:
+        achieved = f64_flops / dom_s / 1e12
+        roofline = dict(bound="fp64", kernel=dom, achieved=achieved, peak=fp64_peak,
+                        unit="TFLOP/s", frac=achieved / fp64_peak, traffic=traffic,
+                        peak_source="FP64 FMA probe measured in this run (no FP64 figure in the "
+                                    "measured-peaks file)",
+                        algorithmic_flops_per_step=f64_flops / args.steps)
+
+    fp64_check = None
+    if mixed and not args.no_fp64_check:
+        i64 = g.XCIntegratorFactory(g.ExecutionSpace.Device, "Replicated", "Default", "GB300-FP64",
+                                    "Default").get_instance(g.functional_type(s["functional"]),
+                                                            ctx["lb"])
+        V64 = np.zeros_like(V)
+        e64 = eval_into(i64, P, V64)  # builds the FP64 plan
+        e64 = eval_into(i64, P, V64)
+        t64 = i64.timings()["compute_ms"] * 1e-3
+        fp64_check = dict(exc_fp64=e64, delta_exc=abs(exc - e64),
+                          max_delta_vxc=float(np.abs(V - V64).max()),
+                          delta_nel=abs(integ.last_nel() - i64.last_nel()),
+                          fp64_value=t64, speedup_vs_fp64=t64 / value,
+                          gates=dict(delta_exc=1e-8, max_delta_vxc=1e-8))
 
     cpu = None
     if not args.no_cpu_baseline:
@@ -328,7 +363,8 @@ def main():
     line = dict(
         metric=METRIC, value=value, unit="s", n_gpus=args.gpus, steps=args.steps,
         warmup=args.warmup, ms_per_step=value * 1e3, higher_is_better=False, scaling="weak",
-        vs_baseline=None, dtype="f64",
+        vs_baseline=None,
+        dtype="bf16 digits (6 x 7 bit FP64 emulation, FP64 accumulate)" if mixed else "f64",
         data="synthetic: seeded water cluster, even-tempered basis, P=CC^T (no dataset)",
         config=dict(workload=WORKLOADS.get(args.config, str(args.config)), config_index=args.config,
                     lwd=args.lwd, nbf=nbf, ntasks=int(stats["ntasks"]), npts=int(stats["npts"]),
@@ -338,6 +374,7 @@ def main():
         e2e=dict(value=e2e, unit="s", h2d_bytes_per_step=nbf * nbf * 8,
                  d2h_bytes_per_step=nbf * nbf * 8 + 16, pinned=pinned),
         roofline=roofline, cpu_baseline=cpu, gpu_launches=launches, clocks=clocks,
+        fp64_check=fp64_check,
         exc=exc, nel=integ.last_nel(),
         kernels={k: dict(ms_per_step=v["ms"] / args.steps, launches_per_step=v["launches"] / args.steps)
                  for k, v in kt.items()},

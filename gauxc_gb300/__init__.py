@@ -409,10 +409,11 @@ class XCIntegrator(_Handle):
         return {n: dict(ms=out[2 * i], launches=int(out[2 * i + 1])) for i, n in enumerate(names)}
 
     def plan_stats(self):
-        out = (ctypes.c_double * 9)()
-        _call(_L.gauxc_gb300_integrator_plan_stats, self._h, out, 9)
+        out = (ctypes.c_double * 11)()
+        _call(_L.gauxc_gb300_integrator_plan_stats, self._h, out, 11)
         keys = ["ntasks", "npts", "npts_pad", "nbatches", "sum_npts_nbe", "sum_npts_nbe2",
-                "sum_pad_npts_nbe2", "scratch_bytes", "gpu_launches"]
+                "sum_pad_npts_nbe2", "scratch_bytes", "gpu_launches", "tensor_flops_x",
+                "tensor_flops_v"]
         return dict(zip(keys, list(out)))
 
 

@@ -525,6 +525,14 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
       for (int n0 = 0; n0 < nu_pad[i]; n0 += kNTile) vi.push_back(OzItem{i, m0, n0, 0, npts_pad[i]});
   }
   if (npb > 0) close_batch(npb);
+  {
+    int npairs = 0;
+    for (int lev = 2; lev <= kLevels; ++lev)
+      for (int i = 1; i <= kSlices; ++i)
+        if (lev - i >= 1 && lev - i <= kSlices) ++npairs;
+    for (const OzItem& q : xi) stats.tensor_flops_x += 2.0 * kMTile * kNTile * (q.k1 - q.k0) * npairs;
+    for (const OzItem& q : vi) stats.tensor_flops_v += 2.0 * kMTile * kNTile * (q.k1 - q.k0) * npairs;
+  }
   stats.nbatches = (int64_t)mbatches_.size();
   stats.scratch_bytes = max_f64 + max_dig;
 
@@ -591,8 +599,8 @@ int64_t DeviceIntegrator::eval_mixed_batches(bool do_vxc) {
       return (int64_t)1;
     });
     launches += timed(3, [&] {
-      launch_ozaki_v(tk_, mp_, v_items_ + b.v_begin, b.v_end - b.v_begin, f64_, dig_, A_, nbf_,
-                     err_, s);
+      launch_ozaki_v(tk_, mp_, v_items_ + b.v_begin, b.v_end - b.v_begin, f64_, dig_, gga_, A_,
+                     nbf_, err_, s);
       return (int64_t)1;
     });
   }

@@ -386,9 +386,9 @@ void launch_ozaki_x(const TasksDev& tk, const MixedPBDev& mp, const OzItem* item
 }
 
 void launch_ozaki_v(const TasksDev& tk, const MixedPBDev& mp, const OzItem* items, int nitems,
-                    const double* f64, const __nv_bfloat16* dig, double* A, int nbf, int* err,
-                    cudaStream_t s) {
-  launch<EPI_V>(tk, mp, items, nitems, f64, dig, false, A, nbf, err, s);
+                    const double* f64, const __nv_bfloat16* dig, bool gga, double* A, int nbf,
+                    int* err, cudaStream_t s) {
+  launch<EPI_V>(tk, mp, items, nitems, f64, dig, gga, A, nbf, err, s);
 }
 
 }  // namespace gb300

@@ -74,8 +74,8 @@ void launch_ozaki_x(const TasksDev& tk, const MixedPBDev& mp, const OzItem* item
                     const double* f64, const __nv_bfloat16* dig, bool gga, double* rho4,
                     int* err, cudaStream_t s);
 void launch_ozaki_v(const TasksDev& tk, const MixedPBDev& mp, const OzItem* items, int nitems,
-                    const double* f64, const __nv_bfloat16* dig, double* A, int nbf, int* err,
-                    cudaStream_t s);
+                    const double* f64, const __nv_bfloat16* dig, bool gga, double* A, int nbf,
+                    int* err, cudaStream_t s);
 
 size_t ozaki_smem_bytes();
 // Tensor-core GEMM self-test (n x n output, K = k); worst relative error.

@@ -691,10 +691,11 @@ int gauxc_gb300_integrator_plan_stats(GauXCStatus* status, const GauXCIntegrator
   int n = 0;
   guarded(status, [&] {
     PlanStats s = integrator_plan_stats(*deref<XCIntegratorHandle>(integrator.ptr));
-    const double v[9] = {(double)s.ntasks, (double)s.npts, (double)s.npts_pad, (double)s.nbatches,
-                         s.sum_npts_nbe, s.sum_npts_nbe2, s.sum_pad_npts_nbe2, s.scratch_bytes,
-                         (double)s.gpu_launches};
-    for (; n < 9 && n < nmax; ++n) out[n] = v[n];
+    const double v[11] = {(double)s.ntasks, (double)s.npts, (double)s.npts_pad,
+                          (double)s.nbatches, s.sum_npts_nbe, s.sum_npts_nbe2,
+                          s.sum_pad_npts_nbe2, s.scratch_bytes, (double)s.gpu_launches,
+                          s.tensor_flops_x, s.tensor_flops_v};
+    for (; n < 11 && n < nmax; ++n) out[n] = v[n];
   });
   return n;
 }

@@ -29,6 +29,7 @@ struct PlanStats {
   double sum_npts_nbe = 0., sum_npts_nbe2 = 0., sum_pad_npts_nbe2 = 0.;
   double scratch_bytes = 0.;
   int64_t gpu_launches = 0;
+  double tensor_flops_x = 0., tensor_flops_v = 0.;  // BF16 MMA flops per call (mixed path)
 };
 
 class DeviceIntegrator;

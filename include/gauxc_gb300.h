@@ -250,7 +250,8 @@ double gauxc_gb300_integrator_last_nel(GauXCStatus* status, const GauXCIntegrato
 int gauxc_gb300_integrator_timings(GauXCStatus* status, const GauXCIntegrator integrator,
                                    double* out, int nmax);
 /* Plan statistics: {ntasks, npts, npts_pad, nbatches, sum npts*nbe, sum npts*nbe^2,
-   sum npts_pad*nbe_pad^2, scratch bytes, kernel launches of the last call}. */
+   sum npts_pad*nbe_pad^2, scratch bytes, kernel launches of the last call,
+   BF16 tensor FLOPs per call of the density and of the VXC GEMMs (mixed path)}. */
 int gauxc_gb300_integrator_plan_stats(GauXCStatus* status, const GauXCIntegrator integrator,
                                       double* out, int nmax);
 
