@@ -752,6 +752,20 @@ void gauxc_gb300_ssf_weights(GauXCStatus* status, int64_t npts, int32_t natoms,
   });
 }
 
+void gauxc_gb300_ssf_weights_noalloc(GauXCStatus* status, int64_t npts, int32_t natoms,
+                                     const double* x, const double* y, const double* z,
+                                     const int32_t* iparent, const double* dist_nearest,
+                                     const double* coords, double* weights, void* stream) {
+  status_init(status);
+  if (npts < 0 || natoms <= 0) return status_fail(status, "invalid sizes");
+  if (npts == 0) return;
+  if (!x || !y || !z || !iparent || !dist_nearest || !coords || !weights)
+    return status_fail(status, "null array argument");
+  guarded(status, [&] {
+    ssf_weights_noalloc(npts, natoms, x, y, z, iparent, dist_nearest, coords, weights, stream);
+  });
+}
+
 void gauxc_gb300_collocation(GauXCStatus* status, const GauXCBasisSet basis, int64_t npts,
                              const double* points, int32_t nshells, const int32_t* shell_list,
                              double* phi, double* dphi_x, double* dphi_y, double* dphi_z) {

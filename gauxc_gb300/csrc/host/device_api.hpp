@@ -65,6 +65,12 @@ void set_device(int dev);
 // SSF weights on the device for every task of the load balancer.
 void molecular_weights_ssf_device(LoadBalancer& lb, RuntimeEnv& rt);
 
+// SSF weights on caller-owned device arrays with the work space in a fixed
+// file-scope device array (no allocation); see ssf_noalloc.cu for the limits.
+void ssf_weights_noalloc(int64_t npts, int natoms, const double* x, const double* y,
+                         const double* z, const int32_t* iparent, const double* dist_nearest,
+                         const double* coords, double* weights, void* stream);
+
 // Stage-level entry points (host arrays in and out, device compute).
 void ssf_weights_device(int64_t npts, int natoms, const double* points, const int32_t* iparent,
                         const double* dist_nearest, const double* coords, double* weights);

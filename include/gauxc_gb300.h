@@ -278,6 +278,23 @@ void gauxc_gb300_ssf_weights(GauXCStatus* status, int64_t npts, int32_t natoms,
                              const double* points, const int32_t* iparent,
                              const double* dist_nearest, const double* coords,
                              double* weights);
+/* SSF weights for callers that cannot allocate device memory (a host code whose
+   own pool already reserved the GPU, or a loop that must not pay for allocator
+   synchronization).  No counterpart in the reference.  Every pointer is a
+   device pointer owned by the caller: x, y, z, iparent (values in [0, natoms)),
+   dist_nearest and weights hold npts entries, coords 3*natoms (xyz
+   interleaved); weights are modified in place, work is queued on `stream`
+   (a cudaStream_t; NULL = default stream) and the call returns without
+   synchronizing.  The work space is one fixed array of 4 Mi doubles (32 MiB)
+   inside the library, kept by every GPU that loads it until exit:
+   natoms*npts + natoms*natoms must not exceed 4194304 (larger requests are
+   rejected; split the points).  All calls share that array, so calls that
+   overlap on the GPU race; the first call on a device looks the array up and
+   should come before any stream capture.  Nothing is allocated or freed. */
+void gauxc_gb300_ssf_weights_noalloc(GauXCStatus* status, int64_t npts, int32_t natoms,
+                                     const double* x, const double* y, const double* z,
+                                     const int32_t* iparent, const double* dist_nearest,
+                                     const double* coords, double* weights, void* stream);
 /* Collocation of the listed shells, host layout eval[ipt*nbe + ibf]; gradients
    when dphi_* are non-null.  Reference: collocation_device.cu (eval_collocation*). */
 void gauxc_gb300_collocation(GauXCStatus* status, const GauXCBasisSet basis, int64_t npts,
