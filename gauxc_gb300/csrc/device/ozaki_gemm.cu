@@ -22,6 +22,7 @@
 #include <stdexcept>
 #include <vector>
 
+#include "ffmath.cuh"
 #include "umma.cuh"
 #include "xc_mixed.cuh"
 
@@ -166,54 +167,74 @@ __global__ void __launch_bounds__(NT, 1)
   umma::fence_after_sync();
 
   if (!failed && nkb > 0) {
-    double* red = reinterpret_cast<double*>(smem);  // operand ring is free now
-    const int row = warp * 32 + lane;               // TMEM lane == tile row
+    const int row = warp * 32 + lane;  // TMEM lane == tile row
     const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
     const double* phi = f64 + mp.f64_off[b];
     const int64_t blk = (int64_t)np * nu_pad;
-    const double* rvec = phi + (gga ? 4 : 1) * blk;
+    const int nq = gga ? 4 : 1;
+    const double* rvec = phi + nq * blk;
     const double* spv = rvec + nu_pad;
     const double* czv = spv + np;
+    const float2* phi2 = reinterpret_cast<const float2*>(czv + nu_pad);
     const int* bfl = tk.bf_list + tk.bf_off[b];
     for (int c = 0; c < kNTile / 16; ++c) {
-      double d[16];
+      // exact float-float sum of the level accumulators
+      float hi[16], lo[16];
 #pragma unroll
-      for (int n = 0; n < 16; ++n) d[n] = 0.;
+      for (int n = 0; n < 16; ++n) hi[n] = lo[n] = 0.f;
 #pragma unroll
       for (int a = 0; a < kAccs; ++a) {
         float v[16];
         umma::tmem_ld16(lane_addr + a * kNTile + c * 16, v);
 #pragma unroll
-        for (int n = 0; n < 16; ++n) d[n] += (double)v[n];
+        for (int n = 0; n < 16; ++n) {
+          float s, e;
+          ff::two_sum(hi[n], v[n], s, e);
+          hi[n] = s;
+          lo[n] += e;
+        }
       }
       if (EPI == EPI_X) {
+        // X'[nu, p] = 2 * 2^-14 * r_nu * s_p * D: a power of two times D
+        float* redf = reinterpret_cast<float*>(smem);  // [q*16+n][2][kMTile+1]
         const int nu = it.m0 + row;
-        const double rr = rvec[nu] * kDigitScale * 2.0;  // RKS: X = 2 P phi
-        const int nq = gga ? 4 : 1;
-        for (int q = 0; q < nq; ++q) {
-          const double* fq = phi + q * blk + (int64_t)nu * np + it.n0 + c * 16;
-          const double fac = q == 0 ? 1.0 : 2.0;
-#pragma unroll
-          for (int n = 0; n < 16; ++n) {
-            const int p = it.n0 + c * 16 + n;
-            red[(q * 16 + n) * (kMTile + 1) + row] = fac * fq[n] * (d[n] * rr * spv[p]);
+        const int er = (int)((((unsigned long long)__double_as_longlong(rvec[nu])) >> 52) & 0x7FF) - 1023;
+        for (int n = 0; n < 16; ++n) {
+          const int p = it.n0 + c * 16 + n;
+          const int esp = (int)((((unsigned long long)__double_as_longlong(spv[p])) >> 52) & 0x7FF) - 1023;
+          const int e = er + esp - 13;
+          const float sc = (e >= -126 && e <= 127) ? __uint_as_float((unsigned)(e + 127) << 23) : 0.f;
+          const float2 X = make_float2(hi[n] * sc, lo[n] * sc);
+          for (int q = 0; q < nq; ++q) {
+            float2 f = phi2[q * blk + (int64_t)nu * np + p];
+            if (q) f = make_float2(2.f * f.x, 2.f * f.y);
+            const float2 t = ff::mul(X, f);
+            redf[((q * 16 + n) * 2 + 0) * (kMTile + 1) + row] = t.x;
+            redf[((q * 16 + n) * 2 + 1) * (kMTile + 1) + row] = t.y;
           }
         }
         __syncthreads();
         for (int e = tid; e < nq * 16; e += NT) {
-          double s = 0.;
-          const double* rp = red + e * (kMTile + 1);
-          for (int m = 0; m < kMTile; ++m) s += rp[m];
+          const float* ph = redf + (e * 2 + 0) * (kMTile + 1);
+          const float* pl = redf + (e * 2 + 1) * (kMTile + 1);
+          float S = 0.f, E = 0.f;
+          for (int m = 0; m < kMTile; ++m) {
+            float s2, e2;
+            ff::two_sum(S, ph[m], s2, e2);
+            S = s2;
+            E += e2 + pl[m];
+          }
           const int q = e / 16, n = e % 16;
           const int64_t g = tk.pt_off[b] + it.n0 + c * 16 + n;
-          atomicAdd(&out[4 * g + q], s);
+          atomicAdd(&out[4 * g + q], (double)S + (double)E);
         }
         __syncthreads();
       } else {
+        double* red = reinterpret_cast<double*>(smem);
 #pragma unroll
         for (int n = 0; n < 16; ++n) {
           const int nu = it.n0 + c * 16 + n;
-          red[row * 17 + n] = d[n] * kDigitScale * czv[nu];
+          red[row * 17 + n] = ((double)hi[n] + (double)lo[n]) * (kDigitScale * czv[nu]);
         }
         __syncthreads();
         for (int e = tid; e < kMTile * 16; e += NT) {

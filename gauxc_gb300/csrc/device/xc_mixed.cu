@@ -2,14 +2,18 @@
 // (slice) generation for P, phi and Z, and the per-point functional.
 //
 // Layouts per point block (np points, nu_pad basis rows, see xc_mixed.cuh):
-//   FP64 (doubles, at f64_off): phi[mu][p] (+ d/dx, d/dy, d/dz), r[nu_pad],
-//     sp[np], cz[nu_pad]
+//   FP64 region (at f64_off): phi[mu][p] (+ d/dx, d/dy, d/dz) in FP64,
+//     r[nu_pad], sp[np], cz[nu_pad], then phi (+ grad) as float-float pairs
 //   digits (bf16, at dig_off): Pd[s][nu][mu], Fd[s][p][mu], FdT[s][mu][p],
 //     Zd[s][nu][p]   (K index contiguous in every GEMM operand)
+// Scales are powers of two taken from IEEE exponent bits and digits come from
+// integer arithmetic on the fixed-point value (ffmath.cuh), so these kernels
+// issue almost no FP64 instructions.
 #include <cuda_bf16.h>
 
 #include <cfloat>
 
+#include "ffmath.cuh"
 #include "functionals.cuh"
 #include "xc_mixed.cuh"
 
@@ -17,26 +21,14 @@ namespace gb300 {
 
 namespace {
 
-// 2^e with 2^(e-1) <= m < 2^e, so |x| / scale < 1; 1 for m == 0.
-__device__ __forceinline__ double pow2_above(double m) {
-  if (!(m > 0.)) return 1.;
-  int e;
-  frexp(m, &e);
-  return ldexp(1.0, e);
+__device__ __forceinline__ int exp_of_pow2(double p) {
+  return (int)(((unsigned long long)__double_as_longlong(p) >> 52) & 0x7FF) - 1023;
 }
 
-// x in (-1, 1): digits d_i = rint(r 2^(7 i)) stored as d_i 2^(-7 (i-1)).
-__device__ __forceinline__ void write_digits(double x, __nv_bfloat16* out, int64_t stride) {
-  double r = x;
-  double up = 128.0, keep = 1.0;
-#pragma unroll
-  for (int i = 0; i < kSlices; ++i) {
-    const double d = rint(r * up);
-    out[i * stride] = __float2bfloat16_rn((float)(d * keep));
-    r -= d / up;
-    up *= 128.0;
-    keep *= (1.0 / 128.0);
-  }
+// digits of v (|v| < 2^es) written as kSlices bf16 values, `stride` apart
+__device__ __forceinline__ void write_digits(double v, int es, __nv_bfloat16* out, int64_t stride) {
+  ff::digits<kSlices>(ff::fixed42(v, es),
+                      [&](int i, float x) { out[i * stride] = __float2bfloat16_rn(x); });
 }
 
 struct PBView {
@@ -44,6 +36,7 @@ struct PBView {
   int64_t blk;
   const double* phi;
   double *r, *sp, *cz;
+  float2* phi2;  // float-float copies of phi (+ grad)
   __nv_bfloat16 *Pd, *Fd, *FdT, *Zd;
 };
 
@@ -61,6 +54,7 @@ __device__ __forceinline__ PBView view(const TasksDev& tk, const MixedPBDev& mp,
   v.r = base + (gga ? 4 : 1) * v.blk;
   v.sp = v.r + v.nu_pad;
   v.cz = v.sp + v.np;
+  v.phi2 = reinterpret_cast<float2*>(v.cz + v.nu_pad);
   const int64_t S = kSlices;
   __nv_bfloat16* d = dig + mp.dig_off[b];
   v.Pd = d;
@@ -75,35 +69,35 @@ __global__ void point_scale_kernel(TasksDev tk, MixedPBDev mp, int b0, double* f
   const int b = b0 + blockIdx.y;
   PBView v = view(tk, mp, b, gga, f64, nullptr);
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < v.np; p += gridDim.x * blockDim.x) {
-    double m = 0.;
-    for (int mu = 0; mu < v.nu; ++mu) m = fmax(m, fabs(v.phi[(int64_t)mu * v.np + p]));
-    v.sp[p] = pow2_above(m);
+    unsigned long long m = 0;
+    for (int mu = 0; mu < v.nu; ++mu) m = max(m, ff::abs_key(v.phi[(int64_t)mu * v.np + p]));
+    v.sp[p] = ff::pow2(ff::scale_exponent(m));
   }
 }
 
 // ---------------------------------------------------------------- phi digits
-// 32 x 32 tiles (mu x p): FdT written along p, Fd written along mu through smem.
+// 32 x 32 tiles (mu x p): FdT written along p, Fd written along mu through
+// smem; float-float copies of phi (+ grad) for the density epilogue.
 __global__ void phi_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const double* f64,
                                   __nv_bfloat16* dig, int gga) {
   __shared__ __nv_bfloat16 t[kSlices][32][34];
   const int b = b0 + blockIdx.y;
   PBView v = view(tk, mp, b, gga, f64, dig);
   const int tmu = v.nu_pad / 32, tp = v.np / 32;
+  const int nq = gga ? 4 : 1;
   for (int tile = blockIdx.x; tile < tmu * tp; tile += gridDim.x) {
     const int mu0 = (tile / tp) * 32, p0 = (tile % tp) * 32;
     for (int r = threadIdx.y; r < 32; r += blockDim.y) {
       const int mu = mu0 + r, p = p0 + threadIdx.x;
-      const double x = v.phi[(int64_t)mu * v.np + p] / v.sp[p];
-      write_digits(x, v.FdT + (int64_t)mu * v.np + p, v.blk);
-      double rr = x, up = 128.0, keep = 1.0;
-#pragma unroll
-      for (int i = 0; i < kSlices; ++i) {
-        const double d = rint(rr * up);
-        t[i][r][threadIdx.x] = __float2bfloat16_rn((float)(d * keep));
-        rr -= d / up;
-        up *= 128.0;
-        keep *= (1.0 / 128.0);
-      }
+      const int64_t o = (int64_t)mu * v.np + p;
+      const double x = v.phi[o];
+      const int es = exp_of_pow2(v.sp[p]);
+      ff::digits<kSlices>(ff::fixed42(x, es), [&](int i, float d) {
+        const __nv_bfloat16 h = __float2bfloat16_rn(d);
+        v.FdT[i * v.blk + o] = h;
+        t[i][r][threadIdx.x] = h;
+      });
+      for (int q = 0; q < nq; ++q) v.phi2[q * v.blk + o] = ff::split(v.phi[q * v.blk + o]);
     }
     __syncthreads();
     for (int r = threadIdx.y; r < 32; r += blockDim.y) {
@@ -116,39 +110,45 @@ __global__ void phi_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const doub
   }
 }
 
+// Maximum of a 64-bit key over the CTA (blockDim.x a multiple of 32, <= 1024).
+__device__ __forceinline__ unsigned long long block_max(unsigned long long m,
+                                                        unsigned long long* red) {
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    unsigned long long x = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0ULL;
+    for (int o = 16; o > 0; o >>= 1) x = max(x, __shfl_xor_sync(0xffffffffu, x, o));
+    if (threadIdx.x == 0) red[0] = x;
+  }
+  __syncthreads();
+  return red[0];
+}
+
 // ---------------------------------------------------------------- P digits
 // One CTA per (row nu, block): gathers P[U_nu, U_mu], row scale, digits.
 __global__ void p_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const double* __restrict__ P,
                                 int nbf, double* f64, __nv_bfloat16* dig, int gga) {
-  __shared__ double red[32];
+  __shared__ unsigned long long red[32];
   const int b = b0 + blockIdx.y;
   PBView v = view(tk, mp, b, gga, f64, dig);
   const int row = blockIdx.x;
   if (row >= v.nu_pad) return;
   const int* bf = tk.bf_list + tk.bf_off[b];
   const int gr = bf[row];
-  double m = 0.;
+  unsigned long long m = 0;
   if (gr >= 0)
     for (int mu = threadIdx.x; mu < v.nu; mu += blockDim.x) {
       const int gc = bf[mu];
-      if (gc >= 0) m = fmax(m, fabs(P[(int64_t)gr * nbf + gc]));
+      if (gc >= 0) m = max(m, ff::abs_key(P[(int64_t)gr * nbf + gc]));
     }
-  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    double x = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.;
-    for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_xor_sync(0xffffffffu, x, o));
-    if (threadIdx.x == 0) red[0] = x;
-  }
-  __syncthreads();
-  const double sc = pow2_above(red[0]);
-  if (threadIdx.x == 0) v.r[row] = sc;
+  const int es = ff::scale_exponent(block_max(m, red));
+  if (threadIdx.x == 0) v.r[row] = ff::pow2(es);
   const int64_t ps = (int64_t)v.nu_pad * v.nu_pad;
   for (int mu = threadIdx.x; mu < v.nu_pad; mu += blockDim.x) {
     const int gc = mu < v.nu ? bf[mu] : -1;
-    const double x = (gr >= 0 && gc >= 0) ? P[(int64_t)gr * nbf + gc] / sc : 0.;
-    write_digits(x, v.Pd + (int64_t)row * v.nu_pad + mu, ps);
+    const double x = (gr >= 0 && gc >= 0) ? P[(int64_t)gr * nbf + gc] : 0.;
+    write_digits(x, es, v.Pd + (int64_t)row * v.nu_pad + mu, ps);
   }
 }
 
@@ -157,7 +157,7 @@ __global__ void p_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const double
 // column scale cz[nu] over the block's points, digits Zd[s][nu][p].
 __global__ void z_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const double4* __restrict__ zc,
                                 double* f64, __nv_bfloat16* dig, int gga) {
-  __shared__ double red[32];
+  __shared__ unsigned long long red[32];
   const int b = b0 + blockIdx.y;
   PBView v = view(tk, mp, b, gga, f64, dig);
   const int row = blockIdx.x;
@@ -170,21 +170,12 @@ __global__ void z_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const double
     if (gga) val += c.y * f[p + v.blk] + c.z * f[p + 2 * v.blk] + c.w * f[p + 3 * v.blk];
     return v.sp[p] * val;
   };
-  double m = 0.;
-  for (int p = threadIdx.x; p < v.np; p += blockDim.x) m = fmax(m, fabs(zval(p)));
-  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    double x = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.;
-    for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_xor_sync(0xffffffffu, x, o));
-    if (threadIdx.x == 0) red[0] = x;
-  }
-  __syncthreads();
-  const double sc = pow2_above(red[0]);
-  if (threadIdx.x == 0) v.cz[row] = sc;
+  unsigned long long m = 0;
+  for (int p = threadIdx.x; p < v.np; p += blockDim.x) m = max(m, ff::abs_key(zval(p)));
+  const int es = ff::scale_exponent(block_max(m, red));
+  if (threadIdx.x == 0) v.cz[row] = ff::pow2(es);
   for (int p = threadIdx.x; p < v.np; p += blockDim.x)
-    write_digits(zval(p) / sc, v.Zd + (int64_t)row * v.np + p, v.blk);
+    write_digits(zval(p), es, v.Zd + (int64_t)row * v.np + p, v.blk);
 }
 
 // ---------------------------------------------------------------- functional

@@ -81,9 +81,11 @@ size_t ozaki_smem_bytes();
 // Tensor-core GEMM self-test (n x n output, K = k); worst relative error.
 double ozaki_selftest(int n, int k);
 
-// Host helpers: workspace sizes of one point block.
+// Host helpers: workspace sizes of one point block.  The FP64 region holds
+// phi (+ grad) in FP64, the scales r[nu_pad], sp[np], cz[nu_pad], then the same
+// phi (+ grad) as float-float pairs (float2, one double's worth each).
 inline int64_t mixed_f64_doubles(int np, int nu_pad, bool gga) {
-  return (int64_t)(gga ? 4 : 1) * np * nu_pad + 2 * nu_pad + np;
+  return 2LL * (gga ? 4 : 1) * np * nu_pad + 2 * nu_pad + np;
 }
 inline int64_t mixed_dig_elems(int np, int nu_pad) {
   return (int64_t)kSlices * ((int64_t)nu_pad * nu_pad + 3LL * np * nu_pad);
