@@ -40,11 +40,11 @@ __device__ __forceinline__ void digits(long long q, Store&& store) {
   float d[S];
 #pragma unroll
   for (int i = S - 1; i > 0; --i) {
-    const long long di = ((q + 64) & 127) - 64;
+    const int di = (int)((q + 64) & 127) - 64;
     d[i] = (float)di;
     q = (q - di) >> 7;
   }
-  d[0] = (float)q;
+  d[0] = (float)(int)q;
   float sc = 1.f;
 #pragma unroll
   for (int i = 0; i < S; ++i) {
@@ -82,6 +82,58 @@ __device__ __forceinline__ float2 mul(float2 a, float2 x) {
   e = fmaf(a.x, x.y, e);
   e = fmaf(a.y, x.x, e);
   return make_float2(p, e);
+}
+
+// 2^e as a float for e in the normal range, 0 below it (and above it, which
+// the callers never reach).
+__device__ __forceinline__ float pow2f(int e) {
+  return (e >= -126 && e <= 127) ? __uint_as_float((unsigned)(e + 127) << 23) : 0.f;
+}
+
+// (hi + lo) * 2^e2 as a double, built with integer arithmetic (no FP64
+// instructions).  Both parts are aligned to the larger exponent with 30 guard
+// bits (error below 2^-54 of the larger part), summed exactly in 64 bits and
+// rounded once to 53 bits.  Results below the double normal range return 0;
+// float subnormal inputs count as 0.
+__device__ __forceinline__ double to_double(float hi, float lo, int e2) {
+  const unsigned hb = __float_as_uint(hi), lb = __float_as_uint(lo);
+  const int eh = (int)((hb >> 23) & 0xFF), el = (int)((lb >> 23) & 0xFF);
+  const int E = eh > el ? eh : el;
+  if (E == 0) return 0.0;
+  long long H = 0, L = 0;
+  if (eh != 0 && E - eh < 55) H = ((long long)((hb & 0x7FFFFFu) | 0x800000u) << 30) >> (E - eh);
+  if (el != 0 && E - el < 55) L = ((long long)((lb & 0x7FFFFFu) | 0x800000u) << 30) >> (E - el);
+  if (hb >> 31) H = -H;
+  if (lb >> 31) L = -L;
+  const long long T = H + L;  // value = T * 2^(E - 180 + e2), |T| < 2^55
+  if (T == 0) return 0.0;
+  const unsigned long long sign = T < 0 ? (1ULL << 63) : 0ULL;
+  unsigned long long M = T < 0 ? (unsigned long long)(-T) : (unsigned long long)T;
+  const int msb = 63 - __clzll((long long)M);
+  int ex = E - 180 + e2;
+  if (msb > 52) {
+    const int sh = msb - 52;
+    M = (M + (1ULL << (sh - 1))) >> sh;
+    ex += sh;
+    if (M >> 53) {
+      M >>= 1;
+      ex += 1;
+    }
+  } else {
+    M <<= (52 - msb);
+    ex -= 52 - msb;
+  }
+  const int be = ex + 52 + 1023;
+  if (be <= 0) return 0.0;
+  if (be >= 2047) return __longlong_as_double((long long)(sign | (0x7FFULL << 52)));
+  return __longlong_as_double((long long)(sign | ((unsigned long long)be << 52) | (M & 0xFFFFFFFFFFFFFULL)));
+}
+
+// a + b for float-float values (hi, lo)
+__device__ __forceinline__ float2 add(float2 a, float2 b) {
+  float s, e;
+  two_sum(a.x, b.x, s, e);
+  return make_float2(s, a.y + b.y + e);
 }
 
 }  // namespace ff

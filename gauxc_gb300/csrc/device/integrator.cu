@@ -92,6 +92,8 @@ struct MBatch {
   int64_t g0, g1;            // point range
   int max_nu_pad;
   int partial_base;
+  int x_sched, x_ncta;       // persistent-launch schedules (offsets into sched_)
+  int v_sched, v_ncta;
 };
 
 }  // namespace
@@ -157,9 +159,11 @@ class DeviceIntegrator {
   std::vector<MBatch> mbatches_;
   OzItem* x_items_ = nullptr;
   OzItem* v_items_ = nullptr;
+  int* sched_ = nullptr;
   double* f64_ = nullptr;
   __nv_bfloat16* dig_ = nullptr;
   double* rho4_ = nullptr;
+  double* prs_ = nullptr;  // row scales of P
   int* err_ = nullptr;
   std::vector<cudaEvent_t> pev_;
   std::vector<int> pev_class_;
@@ -350,11 +354,21 @@ void DeviceIntegrator::build(const LoadBalancer& lb) {
   generation = lb.generation;
 }
 
+// Padded tensor-core work of one point block: density GEMM (M = basis rows
+// padded to kMTile, N = points padded to kNTile, K = basis padded to kBK)
+// plus VXC GEMM (M = basis to kMTile, N = basis to kNTile, K = points).
+static double pb_cost(int npts, int nu) {
+  const double np = (double)round_up(npts, kNTile);
+  const double m = (double)round_up(nu, kMTile), n = (double)round_up(nu, kNTile),
+               k = (double)round_up(nu, kBK);
+  return m * np * k + m * n * np;
+}
+
 // Point blocks for the tensor-core path: consecutive tasks of one parent atom
 // (the load balancer orders them by shell list) are merged while the block
-// holds at most kPBMaxPts points and its union basis stays within 25 % of its
-// largest member's; a task larger than kPBMaxPts points is split.  The union
-// basis is padded to kMTile rows, the points to kNTile columns.
+// holds at most kPBMaxPts points and the padded GEMM work of the merged block
+// does not exceed that of its parts kept apart; a task larger than kPBMaxPts
+// points is split.  Padded extents: PBDims.
 void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
   const BasisSet& bs = *lb.basis;
   cudaStream_t s = stream_;
@@ -386,7 +400,7 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
         std::set_union(b.shells.begin(), b.shells.end(), tt.shell_list.begin(),
                        tt.shell_list.end(), std::back_inserter(u));
         const int nu = nbe_of(u);
-        if (nu * 4 <= std::max(b.nu, tt.nbe) * 5) {
+        if (pb_cost(b.npts + (p1 - p0), nu) <= pb_cost(b.npts, b.nu) + pb_cost(p1 - p0, tt.nbe)) {
           b.shells.swap(u);
           b.nu = nu;
           b.npts += p1 - p0;
@@ -405,14 +419,11 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
       }
     }
   }
-  // largest blocks first (load balance inside each launch)
+  // Blocks stay in atom order: the VXC updates of one atom's blocks then hit
+  // the same rows and columns of the nbf x nbf accumulator while they are
+  // resident in L2, and P's rows are gathered from L2 likewise.
   std::vector<int> order(pbs.size());
   std::iota(order.begin(), order.end(), 0);
-  auto cost = [&](int i) {
-    const double np = (double)round_up(pbs[i].npts, kNTile), nu = (double)round_up(pbs[i].nu, kMTile);
-    return np * nu * nu;
-  };
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost(a) > cost(b); });
 
   const int npb = (int)pbs.size();
   std::vector<int64_t> pt_off(npb), bf_off(npb), sh_off(npb), f64_off(npb), dig_off(npb),
@@ -490,7 +501,7 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
   std::vector<OzItem> xi, vi;
   double f64_used = 0., dig_used = 0., max_f64 = 0., max_dig = 0.;
   const int nfb = functional_partial_blocks();
-  MBatch cur{0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  MBatch cur{0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   auto close_batch = [&](int i) {
     cur.b1 = i;
     cur.coll_end = (int)coll.size();
@@ -501,12 +512,12 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
   };
   for (int i = 0; i < npb; ++i) {
     const double nf = (double)mixed_f64_doubles(npts_pad[i], nu_pad[i], gga_) * 8.;
-    const double nd = (double)mixed_dig_elems(npts_pad[i], nu_pad[i]) * 2.;
+    const double nd = (double)mixed_dig_elems(npts_pad[i], nu[i]) * 2.;
     if (nf + nd > budget) throw error("insufficient device memory for one point block");
     if (f64_used + dig_used + nf + nd > budget && i > cur.b0) {
       close_batch(i);
       cur = MBatch{i, i, (int)coll.size(), 0, (int)xi.size(), 0, (int)vi.size(), 0, pt_off[i], 0,
-                   0, (int)mbatches_.size() * nfb};
+                   0, (int)mbatches_.size() * nfb, 0, 0, 0, 0};
       f64_used = dig_used = 0.;
     }
     f64_off[i] = (int64_t)(f64_used / 8.);
@@ -517,12 +528,13 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
     max_dig = std::max(max_dig, dig_used);
     cur.max_nu_pad = std::max(cur.max_nu_pad, nu_pad[i]);
     for (int b = 0; b < (npts_pad[i] + 127) / 128; ++b) coll.push_back(make_int2(i, b));
-    for (int m0 = 0; m0 < nu_pad[i]; m0 += kMTile)
-      for (int n0 = 0; n0 < npts_pad[i]; n0 += kNTile)
-        for (int k0 = 0; k0 < nu_pad[i]; k0 += kMaxK)
-          xi.push_back(OzItem{i, m0, n0, k0, std::min(k0 + kMaxK, nu_pad[i])});
-    for (int m0 = 0; m0 < nu_pad[i]; m0 += kMTile)
-      for (int n0 = 0; n0 < nu_pad[i]; n0 += kNTile) vi.push_back(OzItem{i, m0, n0, 0, npts_pad[i]});
+    const PBDims d(npts_pad[i], nu[i]);
+    for (int m0 = 0; m0 < d.nu128; m0 += kMTile)
+      for (int n0 = 0; n0 < d.np; n0 += kNTile)
+        for (int k0 = 0; k0 < d.nu16; k0 += kMaxK)
+          xi.push_back(OzItem{i, m0, n0, k0, std::min(k0 + kMaxK, d.nu16)});
+    for (int m0 = 0; m0 < d.nu128; m0 += kMTile)
+      for (int n0 = 0; n0 < d.nu64; n0 += kNTile) vi.push_back(OzItem{i, m0, n0, 0, d.np});
   }
   if (npb > 0) close_batch(npb);
   {
@@ -532,6 +544,17 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
         if (lev - i >= 1 && lev - i <= kSlices) ++npairs;
     for (const OzItem& q : xi) stats.tensor_flops_x += 2.0 * kMTile * kNTile * (q.k1 - q.k0) * npairs;
     for (const OzItem& q : vi) stats.tensor_flops_v += 2.0 * kMTile * kNTile * (q.k1 - q.k0) * npairs;
+  }
+  // per-CTA tile lists of every persistent GEMM launch
+  int nsm = 0, dev = 0;
+  GB300_CUDA(cudaGetDevice(&dev));
+  GB300_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  std::vector<int> sched;
+  for (MBatch& mb : mbatches_) {
+    mb.x_sched = (int)sched.size();
+    mb.x_ncta = ozaki_schedule(xi, mb.x_begin, mb.x_end, nsm, sched);
+    mb.v_sched = (int)sched.size();
+    mb.v_ncta = ozaki_schedule(vi, mb.v_begin, mb.v_end, nsm, sched);
   }
   stats.nbatches = (int64_t)mbatches_.size();
   stats.scratch_bytes = max_f64 + max_dig;
@@ -560,9 +583,11 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
   coll_items_ = arena_.upload(coll, s);
   x_items_ = arena_.upload(xi, s);
   v_items_ = arena_.upload(vi, s);
+  sched_ = arena_.upload(sched, s);
   f64_ = arena_.alloc<double>((size_t)(max_f64 / 8.) + 32);
   dig_ = arena_.alloc<__nv_bfloat16>((size_t)(max_dig / 2.) + 128);
   rho4_ = arena_.alloc<double>((size_t)std::max<int64_t>(pts, 1) * 4);
+  prs_ = arena_.alloc<double>((size_t)nbf_);
   zcoef_ = arena_.alloc<double4>(std::max<int64_t>(pts, 1));
   ndens_ = (int)mbatches_.size() * nfb;
   partials_ = arena_.alloc<double2>(std::max(ndens_, 1));
@@ -571,6 +596,10 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
 int64_t DeviceIntegrator::eval_mixed_batches(bool do_vxc) {
   cudaStream_t s = stream_;
   int64_t launches = 0;
+  launches += timed(4, [&] {
+    launch_p_row_scales(P_, nbf_, prs_, s);
+    return (int64_t)1;
+  });
   for (const MBatch& b : mbatches_) {
     GB300_CUDA(cudaMemsetAsync(rho4_ + 4 * b.g0, 0, (size_t)(b.g1 - b.g0) * 4 * sizeof(double), s));
     launches += timed(0, [&] {
@@ -581,12 +610,12 @@ int64_t DeviceIntegrator::eval_mixed_batches(bool do_vxc) {
     launches += timed(4, [&] {
       launch_point_scales(tk_, mp_, b.b0, b.b1, gga_, f64_, s);
       launch_phi_digits(tk_, mp_, b.b0, b.b1, gga_, f64_, dig_, s);
-      launch_p_digits(tk_, mp_, b.b0, b.b1, b.max_nu_pad, gga_, P_, nbf_, f64_, dig_, s);
+      launch_p_digits(tk_, mp_, b.b0, b.b1, b.max_nu_pad, gga_, P_, prs_, nbf_, f64_, dig_, s);
       return (int64_t)3;
     });
     launches += timed(1, [&] {
-      launch_ozaki_x(tk_, mp_, x_items_ + b.x_begin, b.x_end - b.x_begin, f64_, dig_, gga_, rho4_,
-                     err_, s);
+      launch_ozaki_x(tk_, mp_, OzSchedule{x_items_, sched_ + b.x_sched, b.x_ncta}, f64_, dig_, gga_,
+                     rho4_, err_, s);
       return (int64_t)1;
     });
     launches += timed(4, [&] {
@@ -599,8 +628,8 @@ int64_t DeviceIntegrator::eval_mixed_batches(bool do_vxc) {
       return (int64_t)1;
     });
     launches += timed(3, [&] {
-      launch_ozaki_v(tk_, mp_, v_items_ + b.v_begin, b.v_end - b.v_begin, f64_, dig_, gga_, A_,
-                     nbf_, err_, s);
+      launch_ozaki_v(tk_, mp_, OzSchedule{v_items_, sched_ + b.v_sched, b.v_ncta}, f64_, dig_, gga_,
+                     A_, nbf_, err_, s);
       return (int64_t)1;
     });
   }

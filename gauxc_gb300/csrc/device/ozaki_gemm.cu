@@ -3,23 +3,37 @@
 //
 //  X tile (density): D[nu, p] = sum_mu Pd[nu, mu] Fd[p, mu] over one K chunk;
 //    X'[nu, p] = 2 * 2^-14 * D * r_nu * s_p is contracted on the spot with
-//    phi[nu, p] (rho) and 2 grad phi[nu, p] (grad rho) and reduced over the
-//    tile's 128 basis rows; the four per-point partial sums are added to rho4.
-//    rho is linear in X, so K chunks never need to be summed in X itself.
+//    phi[nu, p] (rho) and 2 grad phi[nu, p] (grad rho); the sums over the
+//    tile's 128 basis rows (TMEM lanes) run as warp reduce-scatters in
+//    float-float arithmetic and each warp adds its per-point partials to
+//    rho4.  rho is linear in X, so K chunks never need to be summed in X.
 //  V tile (VXC): D[mu, nu] = sum_p FdT[mu, p] Zd[nu, p];
 //    A[mu, nu] += 2^-14 * D * cz_nu, scattered with coalesced FP64 atomics.
 //
-// CTA = 128 threads.  All threads stage operand tiles with cp.async into a
-// 3-deep ring of K blocks (BK = 32, kSlices digit tiles of A and B per block);
-// thread 0 issues the MMAs of a block and commits them to the block's
-// mbarrier, which frees the stage for the next load.  The 128 x 64 accumulators
-// of the five levels occupy 320 TMEM columns (512 allocated).  Every mbarrier
-// wait is bounded; on expiry the CTA records an error and leaves after its
-// copies drained and TMEM is released.
+// Persistent, warp-specialised CTAs (one per SM), each walking its own list
+// of tiles:
+//   warp 0    producer: two bulk copies per K block (the operands are stored
+//             in HBM as shared-memory images, xc_mixed.cuh) into a kStages
+//             ring, completion counted on the stage's `full` mbarrier;
+//   warp 1    one lane issues the 21 slice-pair MMAs of a K block and commits
+//             them to the stage's `empty` mbarrier; after a tile's last block
+//             it commits to the TMEM buffer's `tfull` mbarrier;
+//   warps 2-9 epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31, columns
+//             32 ((w - 2) / 4) .. +31 of each accumulator.  Two TMEM buffers
+//             of four level accumulators (2 x 256 columns) let a tile's
+//             epilogue overlap the next tile's main loop; `tempty` hands a
+//             buffer back.
+// Every mbarrier wait is bounded.  On expiry the CTA records an error code,
+// each role leaves its loop, the producer waits (bounded) for its copies in
+// flight, the MMA lane for its MMAs, and TMEM is released.
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cmath>
+#include <queue>
 #include <stdexcept>
+#include <string>
+#include <utility>
 #include <vector>
 
 #include "ffmath.cuh"
@@ -30,251 +44,328 @@ namespace gb300 {
 
 namespace {
 
-constexpr int BK = 32;
-constexpr int NT = 128;
-constexpr int kStages = 3;
-constexpr int kATile = kMTile * BK * 2;   // bytes of one A digit tile (8 KB)
-constexpr int kBTile = kNTile * BK * 2;   // bytes of one B digit tile (4 KB)
-constexpr int kStageBytes = kSlices * (kATile + kBTile);
-constexpr int kAccs = 5;
-constexpr uint32_t kTmemCols = 512;
+constexpr int kStages = 5;
+constexpr int kEpiWarps = 8;  // two per TMEM lane quarter, each on half the columns
+constexpr int kThreads = 64 + 32 * kEpiWarps;
+constexpr int kAccs = 4;
+constexpr int kAPlane = kMTile * kBK * 2;  // bytes of one digit plane of an A tile (4 KB)
+constexpr int kBPlane = kNTile * kBK * 2;  // bytes of one digit plane of a B tile (2 KB)
+constexpr int kABytes = kSlices * kAPlane;
+constexpr int kBBytes = kSlices * kBPlane;
+constexpr int kStageBytes = kABytes + kBBytes;
+constexpr int kAccCols = kAccs * kNTile;  // TMEM columns of one buffer
+constexpr uint32_t kTmemCols = 2 * kAccCols;
+constexpr int kEpiStride = 17;  // padded row of a warp's 32 x 16 transposition tile
+constexpr int kEpiBytes = kEpiWarps * 32 * kEpiStride * 8;
+constexpr int kBarOffset = kStages * kStageBytes + kEpiBytes;
 constexpr uint32_t kWaitLimit = 1u << 22;
 constexpr uint32_t kIdesc = umma::idesc_bf16_f32(kMTile, kNTile);
-constexpr double kDigitScale = 1.0 / 16384.0;  // 2^-14
-
-struct Pair {
-  int8_t i, j, acc;
-};
-// slice pairs (0-based digits) with i + j + 2 <= kLevels, grouped by level
-__constant__ Pair c_pairs[32];
-__constant__ int c_npairs;
+static_assert(kBK == 16, "one MMA (K = 16) per operand tile");
+static_assert(kTmemCols <= 512, "TMEM holds 512 columns");
 
 enum { EPI_X = 0, EPI_V = 1 };
+// error codes: which wait expired
+enum { ERR_EMPTY = 1, ERR_TEMPTY = 2, ERR_FULL = 3, ERR_TFULL = 4 };
+
+struct Bars {
+  uint64_t full[kStages];
+  uint64_t empty[kStages];
+  uint64_t tfull[2];
+  uint64_t tempty[2];
+  uint64_t done;
+  uint32_t tmem_slot;
+  int fail;
+};
+
+__device__ __forceinline__ int exp_of_pow2(double p) {
+  return (int)(((unsigned long long)__double_as_longlong(p) >> 52) & 0x7FF) - 1023;
+}
+
+__device__ __forceinline__ void set_fail(Bars* B, int code) { atomicCAS(&B->fail, 0, code); }
+
+// Failure flag as seen by lane 0, the same in every lane of the warp.
+__device__ __forceinline__ bool warp_failed(const Bars* B) {
+  const int f = *reinterpret_cast<const volatile int*>(&B->fail);
+  return __shfl_sync(0xffffffffu, f, 0) != 0;
+}
+
+// Bounded wait whose outcome is the same in every lane of the warp.
+__device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity) {
+  const bool ok = umma::mbar_wait(bar, parity, kWaitLimit);
+  return __all_sync(0xffffffffu, ok);
+}
+
+// The 21 slice-pair MMAs of one K block: pair (i, j) (0-based digits,
+// i + j + 2 <= kLevels) accumulates into level accumulator min(i + j, 3).
+__device__ __forceinline__ void issue_block(uint32_t d0, uint32_t a0, uint32_t b0, bool acc_prev) {
+#pragma unroll
+  for (int i = 0; i < kSlices; ++i)
+#pragma unroll
+    for (int j = 0; j < kSlices; ++j) {
+      if (i + j + 2 > kLevels) continue;
+      const int acc = i + j < kAccs - 1 ? i + j : kAccs - 1;
+      const bool first = (i == 0) && (j <= kAccs - 1);  // first pair of its accumulator
+      const uint64_t ad = umma::smem_desc(a0 + i * kAPlane, 128, (kBK / 8) * 128);
+      const uint64_t bd = umma::smem_desc(b0 + j * kBPlane, 128, (kBK / 8) * 128);
+      umma::mma_bf16(d0 + acc * kNTile, ad, bd, kIdesc, (acc_prev || !first) ? 1u : 0u);
+    }
+}
+
+// Sum over the 32 lanes of 16 float-float values per lane (reduce-scatter):
+// on return lanes 2k and 2k+1 both hold, in h[0] + l[0], the total of value
+// index 8 b4 + 4 b3 + 2 b2 + b1 (bk = bit k of the lane index).
+__device__ __forceinline__ void reduce16(float (&h)[16], float (&l)[16], int lane) {
+#pragma unroll
+  for (int step = 0; step < 4; ++step) {
+    const int o = 16 >> step;
+    const int half = 8 >> step;
+    const bool up = (lane & o) != 0;
+#pragma unroll
+    for (int i = 0; i < half; ++i) {
+      const float sh = up ? h[i] : h[i + half], sl = up ? l[i] : l[i + half];
+      const float kh = up ? h[i + half] : h[i], kl = up ? l[i + half] : l[i];
+      const float rh = __shfl_xor_sync(0xffffffffu, sh, o);
+      const float rl = __shfl_xor_sync(0xffffffffu, sl, o);
+      const float2 t = ff::add(make_float2(kh, kl), make_float2(rh, rl));
+      h[i] = t.x;
+      l[i] = t.y;
+    }
+  }
+  const float rh = __shfl_xor_sync(0xffffffffu, h[0], 1);
+  const float rl = __shfl_xor_sync(0xffffffffu, l[0], 1);
+  const float2 t = ff::add(make_float2(h[0], l[0]), make_float2(rh, rl));
+  h[0] = t.x;
+  l[0] = t.y;
+}
+
+// Exact float-float sum of the four level accumulators of one column.
+__device__ __forceinline__ float2 sum_levels(float a, float b, float c, float d) {
+  float s, e, s2, e2, s3, e3;
+  ff::two_sum(a, b, s, e);
+  ff::two_sum(s, c, s2, e2);
+  ff::two_sum(s2, d, s3, e3);
+  return make_float2(s3, e + e2 + e3);
+}
+
+// First element of the tile row block holding rows [m0, m0 + TR) of an
+// operand, for EPI's A (M) and B (N) operands.
+template <int EPI>
+__device__ __forceinline__ void operands(const OzItem& it, const TasksDev& tk,
+                                         const MixedPBDev& mp, const __nv_bfloat16* dig,
+                                         const __nv_bfloat16*& A, const __nv_bfloat16*& B) {
+  const int b = it.pb;
+  const PBDims d(tk.npts_pad[b], tk.nbe[b]);
+  const __nv_bfloat16* base = dig + mp.dig_off[b];
+  const int64_t nkb = (EPI == EPI_X ? d.nu16 : d.np) / kBK;
+  A = base + (EPI == EPI_X ? d.pd() : d.fdt()) +
+      (int64_t)(it.m0 / kMTile) * nkb * (kSlices * kMTile * kBK);
+  B = base + (EPI == EPI_X ? d.fd() : d.zd()) +
+      (int64_t)(it.n0 / kNTile) * nkb * (kSlices * kNTile * kBK);
+}
 
 template <int EPI>
-__global__ void __launch_bounds__(NT, 1)
-    ozaki_kernel(TasksDev tk, MixedPBDev mp, const OzItem* __restrict__ items,
-                 const double* __restrict__ f64, const __nv_bfloat16* __restrict__ dig, int gga,
-                 double* __restrict__ out, int nbf, int* __restrict__ err) {
+__global__ void __launch_bounds__(kThreads, 1)
+    ozaki_kernel(TasksDev tk, MixedPBDev mp, OzSchedule sched, const double* __restrict__ f64,
+                 const __nv_bfloat16* __restrict__ dig, int gga, double* __restrict__ out, int nbf,
+                 int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~uintptr_t(1023));
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kStages * kStageBytes);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + kStages);
-
+  Bars* B = reinterpret_cast<Bars*>(smem + kBarOffset);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const OzItem it = items[blockIdx.x];
-  const int b = it.pb;
-  const int np = tk.npts_pad[b];
-  const int nu_pad = tk.nbe_pad[b];
-  const int64_t S = kSlices;
-  const __nv_bfloat16* base = dig + mp.dig_off[b];
-  const __nv_bfloat16 *A, *B;
-  int64_t lda, ldb, a_slice, b_slice;
-  if (EPI == EPI_X) {
-    A = base;
-    lda = nu_pad;
-    a_slice = (int64_t)nu_pad * nu_pad;
-    B = base + S * nu_pad * nu_pad;
-    ldb = nu_pad;
-    b_slice = (int64_t)np * nu_pad;
-  } else {
-    A = base + S * nu_pad * nu_pad + S * (int64_t)np * nu_pad;
-    lda = np;
-    a_slice = (int64_t)nu_pad * np;
-    B = A + S * (int64_t)nu_pad * np;
-    ldb = np;
-    b_slice = (int64_t)nu_pad * np;
-  }
-  const int nkb = (it.k1 - it.k0) / BK;
+  const int beg = sched.cta_off[blockIdx.x], end = sched.cta_off[blockIdx.x + 1];
 
   if (tid == 0) {
-    for (int s = 0; s < kStages; ++s) umma::mbar_init(&bars[s], 1);
+    for (int s = 0; s < kStages; ++s) {
+      umma::mbar_init(&B->full[s], 1);
+      umma::mbar_init(&B->empty[s], 1);
+    }
+    for (int s = 0; s < 2; ++s) {
+      umma::mbar_init(&B->tfull[s], 1);
+      umma::mbar_init(&B->tempty[s], kEpiWarps);
+    }
+    umma::mbar_init(&B->done, 1);
+    B->fail = 0;
     umma::fence_barrier_init();
   }
-  if (warp == 0) umma::tmem_alloc(tmem_slot, kTmemCols);
+  if (warp == 0) umma::tmem_alloc(&B->tmem_slot, kTmemCols);
   umma::fence_before_sync();
   __syncthreads();
   umma::fence_after_sync();
-  const uint32_t tmem = *tmem_slot;
+  const uint32_t tmem = B->tmem_slot;
 
-  auto load_block = [&](int kb) {
-    uint8_t* st = smem + (kb % kStages) * kStageBytes;
-    const int kg = it.k0 + kb * BK;
-    for (int c = tid; c < kSlices * kMTile * (BK / 8); c += NT) {
-      const int s = c / (kMTile * (BK / 8)), rem = c % (kMTile * (BK / 8));
-      const int row = rem / (BK / 8), kc = rem % (BK / 8);
-      umma::cp_async16(st + s * kATile + umma::tile_offset<BK>(row, kc * 8),
-                       A + s * a_slice + (int64_t)(it.m0 + row) * lda + kg + kc * 8);
+  if (warp == 0) {
+    // ------------------------------------------------------------ producer
+    uint32_t g = 0;
+    for (int ii = beg; ii < end; ++ii) {
+      if (warp_failed(B)) break;
+      const OzItem it = sched.items[ii];
+      const __nv_bfloat16 *A, *Bm;
+      operands<EPI>(it, tk, mp, dig, A, Bm);
+      bool ok = true;
+      for (int kb = it.k0 / kBK; kb < it.k1 / kBK; ++kb) {
+        const int st = (int)(g % kStages);
+        if (g >= (uint32_t)kStages && !warp_wait(&B->empty[st], ((g / kStages) - 1) & 1)) {
+          if (lane == 0) set_fail(B, ERR_EMPTY);
+          ok = false;
+          break;
+        }
+        if (lane == 0) {
+          umma::mbar_arrive_expect_tx(&B->full[st], kStageBytes);
+          uint8_t* sa = smem + st * kStageBytes;
+          umma::bulk_g2s(sa, A + (int64_t)kb * (kSlices * kMTile * kBK), kABytes, &B->full[st]);
+          umma::bulk_g2s(sa + kABytes, Bm + (int64_t)kb * (kSlices * kNTile * kBK), kBBytes,
+                         &B->full[st]);
+        }
+        __syncwarp();
+        ++g;
+      }
+      if (!ok) break;
     }
-    uint8_t* stb = st + kSlices * kATile;
-    for (int c = tid; c < kSlices * kNTile * (BK / 8); c += NT) {
-      const int s = c / (kNTile * (BK / 8)), rem = c % (kNTile * (BK / 8));
-      const int row = rem / (BK / 8), kc = rem % (BK / 8);
-      umma::cp_async16(stb + s * kBTile + umma::tile_offset<BK>(row, kc * 8),
-                       B + s * b_slice + (int64_t)(it.n0 + row) * ldb + kg + kc * 8);
-    }
-  };
-
-  bool failed = false;
-  uint32_t acc_init = 0;  // bit a set once accumulator a received its first MMA
-  for (int kb = 0; kb < 2; ++kb) {
-    if (kb < nkb) load_block(kb);
-    umma::cp_async_commit();
-  }
-  for (int kb = 0; kb < nkb; ++kb) {
-    const int nb = kb + 2;
-    bool ok = true;
-    if (nb < nkb) {
-      if (nb >= kStages) ok = umma::mbar_wait(&bars[nb % kStages], ((nb - kStages) / kStages) & 1,
-                                              kWaitLimit);
-      if (ok) load_block(nb);
-    }
-    umma::cp_async_commit();
-    if (__syncthreads_or(!ok)) {
-      failed = true;
-      break;
-    }
-    umma::cp_async_wait<2>();
-    umma::fence_proxy_async_smem();
-    __syncthreads();
-    if (tid == 0) {
+    // copies still in flight land before the CTA leaves
+    for (uint32_t x = g > (uint32_t)kStages ? g - kStages : 0; x < g; ++x)
+      warp_wait(&B->full[x % kStages], (x / kStages) & 1);
+  } else if (warp == 1) {
+    // ------------------------------------------------------------ MMA issue
+    uint32_t g = 0;
+    int li = 0;
+    for (int ii = beg; ii < end; ++ii, ++li) {
+      if (warp_failed(B)) break;
+      const OzItem it = sched.items[ii];
+      const int buf = li & 1;
+      if (li >= 2 && !warp_wait(&B->tempty[buf], ((li >> 1) - 1) & 1)) {
+        if (lane == 0) set_fail(B, ERR_TEMPTY);
+        break;
+      }
       umma::fence_after_sync();
-      const uint8_t* st = smem + (kb % kStages) * kStageBytes;
-      const uint32_t a0 = umma::smem_u32(st), b0 = umma::smem_u32(st + kSlices * kATile);
-      for (int q = 0; q < c_npairs; ++q) {
-        const Pair pr = c_pairs[q];
-#pragma unroll
-        for (int kk = 0; kk < BK / 16; ++kk) {
-          const uint64_t ad = umma::smem_desc(a0 + pr.i * kATile + kk * 256, 128, (BK / 8) * 128);
-          const uint64_t bd = umma::smem_desc(b0 + pr.j * kBTile + kk * 256, 128, (BK / 8) * 128);
-          const uint32_t accum = (acc_init >> pr.acc) & 1u;
-          umma::mma_bf16(tmem + pr.acc * kNTile, ad, bd, kIdesc, accum);
-          acc_init |= 1u << pr.acc;
+      const uint32_t d0 = tmem + buf * kAccCols;
+      const int nkb = (it.k1 - it.k0) / kBK;
+      bool ok = true;
+      for (int kb = 0; kb < nkb; ++kb, ++g) {
+        const int st = (int)(g % kStages);
+        if (!warp_wait(&B->full[st], (g / kStages) & 1)) {
+          if (lane == 0) set_fail(B, ERR_FULL);
+          ok = false;
+          break;
         }
+        umma::fence_after_sync();
+        if (lane == 0) {
+          const uint32_t a0 = umma::smem_u32(smem + st * kStageBytes);
+          issue_block(d0, a0, a0 + kABytes, kb > 0);
+          umma::mma_commit(&B->empty[st]);
+        }
+        __syncwarp();
       }
-      umma::mma_commit(&bars[kb % kStages]);
+      if (!ok) break;
+      if (lane == 0) umma::mma_commit(&B->tfull[buf]);
+      __syncwarp();
     }
-  }
-  // all MMAs done once the last block's commit arrived
-  if (!failed && nkb > 0) {
-    const int last = nkb - 1;
-    const bool ok = umma::mbar_wait(&bars[last % kStages], (last / kStages) & 1, kWaitLimit);
-    if (__syncthreads_or(!ok)) failed = true;
-  }
-  umma::cp_async_wait_all();
-  __syncthreads();
-  umma::fence_after_sync();
-
-  if (!failed && nkb > 0) {
-    const int row = warp * 32 + lane;  // TMEM lane == tile row
-    const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
-    const double* phi = f64 + mp.f64_off[b];
-    const int64_t blk = (int64_t)np * nu_pad;
+    // every MMA issued above has completed before TMEM is released
+    if (lane == 0) umma::mma_commit(&B->done);
+    __syncwarp();
+    warp_wait(&B->done, 0);
+  } else {
+    // ------------------------------------------------------------ epilogue
+    const int q4 = warp & 3;  // TMEM lane quarter this warp may access
+    const int c0 = ((warp - 2) >> 2) * 2;  // first of this warp's two 16-column chunks
+    const int row = q4 * 32 + lane;
+    const uint32_t lane_base = tmem + ((uint32_t)(q4 * 32) << 16);
+    double* red = reinterpret_cast<double*>(smem + kStages * kStageBytes) + (warp - 2) * 32 * kEpiStride;
     const int nq = gga ? 4 : 1;
-    const double* rvec = phi + nq * blk;
-    const double* spv = rvec + nu_pad;
-    const double* czv = spv + np;
-    const float2* phi2 = reinterpret_cast<const float2*>(czv + nu_pad);
-    const int* bfl = tk.bf_list + tk.bf_off[b];
-    for (int c = 0; c < kNTile / 16; ++c) {
-      // exact float-float sum of the level accumulators
-      float hi[16], lo[16];
-#pragma unroll
-      for (int n = 0; n < 16; ++n) hi[n] = lo[n] = 0.f;
-#pragma unroll
-      for (int a = 0; a < kAccs; ++a) {
-        float v[16];
-        umma::tmem_ld16(lane_addr + a * kNTile + c * 16, v);
-#pragma unroll
-        for (int n = 0; n < 16; ++n) {
-          float s, e;
-          ff::two_sum(hi[n], v[n], s, e);
-          hi[n] = s;
-          lo[n] += e;
-        }
+    int li = 0;
+    for (int ii = beg; ii < end; ++ii, ++li) {
+      if (warp_failed(B)) break;
+      const OzItem it = sched.items[ii];
+      const int buf = li & 1;
+      if (!warp_wait(&B->tfull[buf], (li >> 1) & 1)) {
+        if (lane == 0) set_fail(B, ERR_TFULL);
+        break;
       }
+      umma::fence_after_sync();
+      const int b = it.pb;
+      const PBDims d(tk.npts_pad[b], tk.nbe[b]);
+      const int64_t blk = (int64_t)d.np * d.nu128;
+      const double* base = f64 + mp.f64_off[b];
+      const double* rvec = base + nq * blk;
+      const double* spv = rvec + d.nu128;
+      const double* czv = spv + d.np;
+      const uint32_t tb = lane_base + buf * kAccCols;
       if (EPI == EPI_X) {
-        // X'[nu, p] = 2 * 2^-14 * r_nu * s_p * D: a power of two times D
-        float* redf = reinterpret_cast<float*>(smem);  // [q*16+n][2][kMTile+1]
+        const float2* phi2 = reinterpret_cast<const float2*>(czv + d.nu128);
         const int nu = it.m0 + row;
-        const int er = (int)((((unsigned long long)__double_as_longlong(rvec[nu])) >> 52) & 0x7FF) - 1023;
-        for (int n = 0; n < 16; ++n) {
-          const int p = it.n0 + c * 16 + n;
-          const int esp = (int)((((unsigned long long)__double_as_longlong(spv[p])) >> 52) & 0x7FF) - 1023;
-          const int e = er + esp - 13;
-          const float sc = (e >= -126 && e <= 127) ? __uint_as_float((unsigned)(e + 127) << 23) : 0.f;
-          const float2 X = make_float2(hi[n] * sc, lo[n] * sc);
-          for (int q = 0; q < nq; ++q) {
-            float2 f = phi2[q * blk + (int64_t)nu * np + p];
-            if (q) f = make_float2(2.f * f.x, 2.f * f.y);
-            const float2 t = ff::mul(X, f);
-            redf[((q * 16 + n) * 2 + 0) * (kMTile + 1) + row] = t.x;
-            redf[((q * 16 + n) * 2 + 1) * (kMTile + 1) + row] = t.y;
-          }
-        }
-        __syncthreads();
-        for (int e = tid; e < nq * 16; e += NT) {
-          const float* ph = redf + (e * 2 + 0) * (kMTile + 1);
-          const float* pl = redf + (e * 2 + 1) * (kMTile + 1);
-          float S = 0.f, E = 0.f;
-          for (int m = 0; m < kMTile; ++m) {
-            float s2, e2;
-            ff::two_sum(S, ph[m], s2, e2);
-            S = s2;
-            E += e2 + pl[m];
-          }
-          const int q = e / 16, n = e % 16;
-          const int64_t g = tk.pt_off[b] + it.n0 + c * 16 + n;
-          atomicAdd(&out[4 * g + q], (double)S + (double)E);
-        }
-        __syncthreads();
-      } else {
-        double* red = reinterpret_cast<double*>(smem);
+        const int er = exp_of_pow2(rvec[nu]);
+        const int64_t g0 = tk.pt_off[b] + it.n0;
+        for (int c = c0; c < c0 + 2; ++c) {
+          float v[4][16];
+          umma::tmem_ld16x4(tb + c * 16, tb + kNTile + c * 16, tb + 2 * kNTile + c * 16,
+                            tb + 3 * kNTile + c * 16, v);
+          // X'[nu, p] = 2^(er + esp - 13) D, a power of two times D
+          float hi[16], lo[16];
 #pragma unroll
-        for (int n = 0; n < 16; ++n) {
-          const int nu = it.n0 + c * 16 + n;
-          red[row * 17 + n] = ((double)hi[n] + (double)lo[n]) * (kDigitScale * czv[nu]);
+          for (int n = 0; n < 16; ++n) {
+            const float2 t = sum_levels(v[0][n], v[1][n], v[2][n], v[3][n]);
+            const float sc = ff::pow2f(er + exp_of_pow2(spv[it.n0 + c * 16 + n]) - 13);
+            hi[n] = t.x * sc;
+            lo[n] = t.y * sc;
+          }
+          for (int q = 0; q < nq; ++q) {
+            float h[16], l[16];
+            const float2* f = phi2 + q * blk + (int64_t)(it.n0 + c * 16) * d.nu128 + nu;
+#pragma unroll
+            for (int n = 0; n < 16; ++n) {
+              float2 fv = f[(int64_t)n * d.nu128];
+              if (q) fv = make_float2(2.f * fv.x, 2.f * fv.y);
+              const float2 t = ff::mul(make_float2(hi[n], lo[n]), fv);
+              h[n] = t.x;
+              l[n] = t.y;
+            }
+            reduce16(h, l, lane);
+            if ((lane & 1) == 0) {
+              const int n = ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 +
+                            ((lane >> 1) & 1);
+              atomicAdd(&out[4 * (g0 + c * 16 + n) + q], ff::to_double(h[0], l[0], 0));
+            }
+          }
         }
-        __syncthreads();
-        for (int e = tid; e < kMTile * 16; e += NT) {
-          const int m = e / 16, n = e % 16;
-          const int gm = bfl[it.m0 + m], gn = bfl[it.n0 + c * 16 + n];
-          if (gm >= 0 && gn >= 0) atomicAdd(&out[(int64_t)gm * nbf + gn], red[m * 17 + n]);
+      } else {
+        const int* bfl = tk.bf_list + tk.bf_off[b];
+        for (int c = c0; c < c0 + 2; ++c) {
+          float v[4][16];
+          umma::tmem_ld16x4(tb + c * 16, tb + kNTile + c * 16, tb + 2 * kNTile + c * 16,
+                            tb + 3 * kNTile + c * 16, v);
+#pragma unroll
+          for (int n = 0; n < 16; ++n) {
+            const float2 t = sum_levels(v[0][n], v[1][n], v[2][n], v[3][n]);
+            const int ecz = exp_of_pow2(czv[it.n0 + c * 16 + n]);
+            red[lane * kEpiStride + n] = ff::to_double(t.x, t.y, ecz - 14);
+          }
+          __syncwarp();
+          const int n = lane & 15;
+          const int gn = bfl[it.n0 + c * 16 + n];
+          for (int r2 = lane >> 4; r2 < 32; r2 += 2) {
+            const int gm = bfl[it.m0 + q4 * 32 + r2];
+            if (gm >= 0 && gn >= 0) atomicAdd(&out[(int64_t)gm * nbf + gn], red[r2 * kEpiStride + n]);
+          }
+          __syncwarp();
         }
-        __syncthreads();
       }
+      umma::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) umma::mbar_arrive(&B->tempty[buf]);
     }
   }
-  if (failed && tid == 0) atomicExch(err, 1);
+
   umma::fence_before_sync();
   __syncthreads();
+  if (tid == 0 && B->fail) atomicExch(err, B->fail);
+  umma::fence_after_sync();
   if (warp == 0) umma::tmem_dealloc(tmem, kTmemCols);
 }
 
-bool g_pairs_ready = false;
-
-void upload_pairs() {
-  if (g_pairs_ready) return;
-  Pair h[32];
-  int n = 0;
-  for (int lev = 2; lev <= kLevels; ++lev)
-    for (int i = 1; i <= kSlices; ++i) {
-      const int j = lev - i;
-      if (j < 1 || j > kSlices) continue;
-      h[n++] = Pair{(int8_t)(i - 1), (int8_t)(j - 1), (int8_t)(lev - 2 < kAccs - 1 ? lev - 2 : kAccs - 1)};
-    }
-  GB300_CUDA(cudaMemcpyToSymbol(c_pairs, h, sizeof(Pair) * n));
-  GB300_CUDA(cudaMemcpyToSymbol(c_npairs, &n, sizeof(int)));
-  g_pairs_ready = true;
-}
-
 template <int EPI>
-void launch(const TasksDev& tk, const MixedPBDev& mp, const OzItem* items, int nitems,
-            const double* f64, const __nv_bfloat16* dig, bool gga, double* out, int nbf, int* err,
-            cudaStream_t s) {
-  if (!nitems) return;
-  upload_pairs();
+void launch(const TasksDev& tk, const MixedPBDev& mp, const OzSchedule& sched, const double* f64,
+            const __nv_bfloat16* dig, bool gga, double* out, int nbf, int* err, cudaStream_t s) {
+  if (sched.ncta <= 0) return;
   const size_t smem = ozaki_smem_bytes();
   static bool attr[2] = {false, false};
   if (!attr[EPI]) {
@@ -282,30 +373,65 @@ void launch(const TasksDev& tk, const MixedPBDev& mp, const OzItem* items, int n
                                     (int)smem));
     attr[EPI] = true;
   }
-  ozaki_kernel<EPI><<<nitems, NT, smem, s>>>(tk, mp, items, f64, dig, gga ? 1 : 0, out, nbf, err);
+  ozaki_kernel<EPI><<<sched.ncta, kThreads, smem, s>>>(tk, mp, sched, f64, dig, gga ? 1 : 0, out,
+                                                       nbf, err);
   GB300_CUDA(cudaGetLastError());
 }
 
 }  // namespace
 
-size_t ozaki_smem_bytes() { return (size_t)kStages * kStageBytes + 128 + 1024; }
+size_t ozaki_smem_bytes() { return (size_t)kBarOffset + sizeof(Bars) + 1024; }
+
+int ozaki_schedule(std::vector<OzItem>& items, size_t begin, size_t end, int nsm,
+                   std::vector<int>& cta_off) {
+  const size_t n = end - begin;
+  if (n == 0) {
+    cta_off.push_back((int)begin);
+    return 0;
+  }
+  const int ncta = (int)std::min<size_t>((size_t)std::max(nsm, 1), n);
+  // cost of a tile in K blocks, plus a fixed share for its epilogue
+  auto cost = [](const OzItem& q) { return (q.k1 - q.k0) / kBK + 2; };
+  // tiles keep their list order (point blocks in atom order), so the CTAs
+  // advance through the atoms together and their output updates share L2
+  const std::vector<OzItem> v(items.begin() + begin, items.begin() + end);
+  using Load = std::pair<long long, int>;
+  std::priority_queue<Load, std::vector<Load>, std::greater<Load>> heap;
+  for (int c = 0; c < ncta; ++c) heap.push({0LL, c});
+  std::vector<std::vector<OzItem>> lists(ncta);
+  for (const OzItem& q : v) {
+    Load l = heap.top();
+    heap.pop();
+    lists[l.second].push_back(q);
+    l.first += cost(q);
+    heap.push(l);
+  }
+  size_t at = begin;
+  for (int c = 0; c < ncta; ++c) {
+    cta_off.push_back((int)at);
+    for (const OzItem& q : lists[c]) items[at++] = q;
+  }
+  cta_off.push_back((int)at);
+  return ncta;
+}
 
 // Self-test of the VXC-tile GEMM: C[mu][nu] = sum_p F[mu][p] Z[nu][p] for
 // seeded random F in (-1, 1) and Z with row scales spanning 2^-20..2^20,
-// digits built on the host, compared against an FP64 product.  Returns the
-// largest |C - C_ref| / max|C_ref row|.
+// digits built on the host in the tiled operand layout, compared against an
+// FP64 product.  Returns the largest |C - C_ref| / max|C_ref row|.
 double ozaki_selftest(int n, int k) {
   if (n % kMTile || k % kNTile || k > kMaxK) throw std::runtime_error("selftest sizes");
-  const int nu_pad = n, np = k;
-  const int64_t S = kSlices, blk = (int64_t)np * nu_pad;
+  const PBDims d(k, n);
+  const int np = k;
+  const int64_t blk = (int64_t)np * d.nu128;
   uint64_t st = 12345;
   auto rnd = [&]() {
     st = st * 6364136223846793005ULL + 1442695040888963407ULL;
     return ((st >> 11) * (1.0 / 9007199254740992.0)) * 2.0 - 1.0;
   };
-  std::vector<double> F(blk), Z(blk), cz(nu_pad);
+  std::vector<double> F(blk), Z(blk), cz(d.nu128);
   for (auto& x : F) x = rnd() * 0.999;
-  for (int r = 0; r < nu_pad; ++r) {
+  for (int r = 0; r < n; ++r) {
     const double sc = std::ldexp(1.0, (int)(rnd() * 20));
     double m = 0.;
     for (int p = 0; p < np; ++p) {
@@ -316,54 +442,58 @@ double ozaki_selftest(int n, int k) {
     std::frexp(m, &e);
     cz[r] = std::ldexp(1.0, e);
   }
-  auto digits = [&](double x, std::vector<__nv_bfloat16>& out, int64_t at, int64_t stride) {
+  std::vector<__nv_bfloat16> dig(d.dig_elems(), __float2bfloat16_rn(0.f));
+  auto digits = [&](double x, int64_t at, int64_t plane) {
     double r = x, up = 128.0, keep = 1.0;
     for (int i = 0; i < kSlices; ++i) {
-      const double d = std::rint(r * up);
-      out[at + i * stride] = __float2bfloat16_rn((float)(d * keep));
-      r -= d / up;
+      const double dd = std::rint(r * up);
+      dig[at + i * plane] = __float2bfloat16_rn((float)(dd * keep));
+      r -= dd / up;
       up *= 128.0;
       keep /= 128.0;
     }
   };
-  const int64_t off_fdt = S * nu_pad * nu_pad + S * blk, off_zd = off_fdt + S * blk;
-  std::vector<__nv_bfloat16> dig(off_zd + S * blk, __float2bfloat16_rn(0.f));
-  for (int r = 0; r < nu_pad; ++r)
+  for (int r = 0; r < n; ++r)
     for (int p = 0; p < np; ++p) {
-      digits(F[(int64_t)r * np + p], dig, off_fdt + (int64_t)r * np + p, blk);
-      digits(Z[(int64_t)r * np + p] / cz[r], dig, off_zd + (int64_t)r * np + p, blk);
+      digits(F[(int64_t)r * np + p], d.fdt() + oz_offset(0, r, p, kMTile, np), kMTile * kBK);
+      digits(Z[(int64_t)r * np + p] / cz[r], d.zd() + oz_offset(0, r, p, kNTile, np), kNTile * kBK);
     }
-  std::vector<double> f64(blk + 2 * nu_pad + np, 0.);
-  for (int r = 0; r < nu_pad; ++r) f64[blk + nu_pad + np + r] = cz[r];
-  std::vector<int> bf(nu_pad);
-  for (int i = 0; i < nu_pad; ++i) bf[i] = i;
+  // FP64 region: phi block, r[nu128], sp[np], cz[nu128]
+  std::vector<double> f64(blk + 2 * d.nu128 + np, 0.);
+  for (int r = 0; r < n; ++r) f64[blk + d.nu128 + np + r] = cz[r];
+  std::vector<int> bf(d.nu128);
+  for (int i = 0; i < d.nu128; ++i) bf[i] = i;
   std::vector<OzItem> items;
-  for (int m0 = 0; m0 < nu_pad; m0 += kMTile)
-    for (int n0 = 0; n0 < nu_pad; n0 += kNTile) items.push_back(OzItem{0, m0, n0, 0, np});
+  for (int m0 = 0; m0 < d.nu128; m0 += kMTile)
+    for (int n0 = 0; n0 < d.nu64; n0 += kNTile) items.push_back(OzItem{0, m0, n0, 0, np});
+  std::vector<int> cta_off;
+  const int ncta = ozaki_schedule(items, 0, items.size(), 148, cta_off);
   int zero_i = 0;
   int64_t zero_l = 0;
   __nv_bfloat16* ddig;
   double *df64, *dA;
-  int *dbf, *dnp, *dnu, *derr;
+  int *dbf, *dnp, *dnu, *derr, *doffs;
   int64_t *doff, *dz;
   OzItem* ditems;
   GB300_CUDA(cudaMalloc(&ddig, dig.size() * 2));
   GB300_CUDA(cudaMalloc(&df64, f64.size() * 8));
   GB300_CUDA(cudaMalloc(&dA, (size_t)n * n * 8));
-  GB300_CUDA(cudaMalloc(&dbf, nu_pad * 4));
+  GB300_CUDA(cudaMalloc(&dbf, d.nu128 * 4));
   GB300_CUDA(cudaMalloc(&dnp, 4));
   GB300_CUDA(cudaMalloc(&dnu, 4));
   GB300_CUDA(cudaMalloc(&derr, 4));
+  GB300_CUDA(cudaMalloc(&doffs, cta_off.size() * 4));
   GB300_CUDA(cudaMalloc(&doff, 8));
   GB300_CUDA(cudaMalloc(&dz, 8));
   GB300_CUDA(cudaMalloc(&ditems, items.size() * sizeof(OzItem)));
   GB300_CUDA(cudaMemcpy(ddig, dig.data(), dig.size() * 2, cudaMemcpyHostToDevice));
   GB300_CUDA(cudaMemcpy(df64, f64.data(), f64.size() * 8, cudaMemcpyHostToDevice));
   GB300_CUDA(cudaMemset(dA, 0, (size_t)n * n * 8));
-  GB300_CUDA(cudaMemcpy(dbf, bf.data(), nu_pad * 4, cudaMemcpyHostToDevice));
+  GB300_CUDA(cudaMemcpy(dbf, bf.data(), d.nu128 * 4, cudaMemcpyHostToDevice));
   GB300_CUDA(cudaMemcpy(dnp, &np, 4, cudaMemcpyHostToDevice));
-  GB300_CUDA(cudaMemcpy(dnu, &nu_pad, 4, cudaMemcpyHostToDevice));
+  GB300_CUDA(cudaMemcpy(dnu, &n, 4, cudaMemcpyHostToDevice));
   GB300_CUDA(cudaMemcpy(derr, &zero_i, 4, cudaMemcpyHostToDevice));
+  GB300_CUDA(cudaMemcpy(doffs, cta_off.data(), cta_off.size() * 4, cudaMemcpyHostToDevice));
   GB300_CUDA(cudaMemcpy(doff, &zero_l, 8, cudaMemcpyHostToDevice));
   GB300_CUDA(cudaMemcpy(dz, &zero_l, 8, cudaMemcpyHostToDevice));
   GB300_CUDA(cudaMemcpy(ditems, items.data(), items.size() * sizeof(OzItem), cudaMemcpyHostToDevice));
@@ -375,15 +505,16 @@ double ozaki_selftest(int n, int k) {
   tk.bf_list = dbf;
   tk.pt_off = dz;
   MixedPBDev mp{doff, doff};
-  launch<EPI_V>(tk, mp, ditems, (int)items.size(), df64, ddig, false, dA, n, derr, 0);
+  launch<EPI_V>(tk, mp, OzSchedule{ditems, doffs, ncta}, df64, ddig, false, dA, n, derr, 0);
   GB300_CUDA(cudaDeviceSynchronize());
   std::vector<double> C((size_t)n * n);
   int herr = 0;
   GB300_CUDA(cudaMemcpy(C.data(), dA, C.size() * 8, cudaMemcpyDeviceToHost));
   GB300_CUDA(cudaMemcpy(&herr, derr, 4, cudaMemcpyDeviceToHost));
   cudaFree(ddig); cudaFree(df64); cudaFree(dA); cudaFree(dbf); cudaFree(dnp); cudaFree(dnu);
-  cudaFree(derr); cudaFree(doff); cudaFree(dz); cudaFree(ditems);
-  if (herr) throw std::runtime_error("selftest: pipeline wait expired");
+  cudaFree(derr); cudaFree(doffs); cudaFree(doff); cudaFree(dz); cudaFree(ditems);
+  if (herr)
+    throw std::runtime_error("selftest: a pipeline wait expired (code " + std::to_string(herr) + ")");
   double worst = 0.;
   for (int mu = 0; mu < n; ++mu) {
     std::vector<double> ref(n);
@@ -400,16 +531,16 @@ double ozaki_selftest(int n, int k) {
   return worst;
 }
 
-void launch_ozaki_x(const TasksDev& tk, const MixedPBDev& mp, const OzItem* items, int nitems,
+void launch_ozaki_x(const TasksDev& tk, const MixedPBDev& mp, const OzSchedule& sched,
                     const double* f64, const __nv_bfloat16* dig, bool gga, double* rho4, int* err,
                     cudaStream_t s) {
-  launch<EPI_X>(tk, mp, items, nitems, f64, dig, gga, rho4, 0, err, s);
+  launch<EPI_X>(tk, mp, sched, f64, dig, gga, rho4, 0, err, s);
 }
 
-void launch_ozaki_v(const TasksDev& tk, const MixedPBDev& mp, const OzItem* items, int nitems,
+void launch_ozaki_v(const TasksDev& tk, const MixedPBDev& mp, const OzSchedule& sched,
                     const double* f64, const __nv_bfloat16* dig, bool gga, double* A, int nbf,
                     int* err, cudaStream_t s) {
-  launch<EPI_V>(tk, mp, items, nitems, f64, dig, gga, A, nbf, err, s);
+  launch<EPI_V>(tk, mp, sched, f64, dig, gga, A, nbf, err, s);
 }
 
 }  // namespace gb300

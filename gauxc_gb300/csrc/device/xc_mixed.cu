@@ -1,11 +1,13 @@
 // Mixed-precision path, element-wise kernels: power-of-two scales, digit
 // (slice) generation for P, phi and Z, and the per-point functional.
 //
-// Layouts per point block (np points, nu_pad basis rows, see xc_mixed.cuh):
-//   FP64 region (at f64_off): phi[mu][p] (+ d/dx, d/dy, d/dz) in FP64,
-//     r[nu_pad], sp[np], cz[nu_pad], then phi (+ grad) as float-float pairs
-//   digits (bf16, at dig_off): Pd[s][nu][mu], Fd[s][p][mu], FdT[s][mu][p],
-//     Zd[s][nu][p]   (K index contiguous in every GEMM operand)
+// Layouts per point block (PBDims d: np points, nu basis functions):
+//   FP64 region (at f64_off): phi[q][mu][p] (q = value, d/dx, d/dy, d/dz;
+//     nu128 rows) in FP64, r[nu128], sp[np], cz[nu128], then phi2[q][p][mu],
+//     the same values transposed as float-float pairs
+//   digits (bf16, at dig_off): Pd, Fd, FdT, Zd in the tiled operand layout of
+//     xc_mixed.cuh (oz_offset); every thread writes 8 consecutive K entries
+//     of one row, i.e. one 16-byte row of a core matrix per digit plane
 // Scales are powers of two taken from IEEE exponent bits and digits come from
 // integer arithmetic on the fixed-point value (ffmath.cuh), so these kernels
 // issue almost no FP64 instructions.
@@ -25,145 +27,202 @@ __device__ __forceinline__ int exp_of_pow2(double p) {
   return (int)(((unsigned long long)__double_as_longlong(p) >> 52) & 0x7FF) - 1023;
 }
 
-// digits of v (|v| < 2^es) written as kSlices bf16 values, `stride` apart
-__device__ __forceinline__ void write_digits(double v, int es, __nv_bfloat16* out, int64_t stride) {
-  ff::digits<kSlices>(ff::fixed42(v, es),
-                      [&](int i, float x) { out[i * stride] = __float2bfloat16_rn(x); });
+// Digits of 8 values x[e] (|x[e]| < 2^es[e]) stored as kSlices 16-byte rows:
+// plane i at out + i * plane.
+__device__ __forceinline__ void store_digits8(const double (&x)[8], const int (&es)[8],
+                                              __nv_bfloat16* out, int64_t plane) {
+  uint32_t w[kSlices][4];
+#pragma unroll
+  for (int e = 0; e < 8; ++e)
+    ff::digits<kSlices>(ff::fixed42(x[e], es[e]), [&](int i, float dv) {
+      const uint32_t h = __bfloat16_as_ushort(__float2bfloat16_rn(dv));
+      if (e & 1)
+        w[i][e >> 1] |= h << 16;
+      else
+        w[i][e >> 1] = h;
+    });
+#pragma unroll
+  for (int i = 0; i < kSlices; ++i)
+    __stcs(reinterpret_cast<uint4*>(out + i * plane), make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]));
 }
 
 struct PBView {
-  int np, nu, nu_pad;
-  int64_t blk;
+  PBDims d;
+  int64_t blk;  // np * nu128
   const double* phi;
   double *r, *sp, *cz;
-  float2* phi2;  // float-float copies of phi (+ grad)
+  float2* phi2;  // [q][p][mu]
   __nv_bfloat16 *Pd, *Fd, *FdT, *Zd;
+  __device__ PBView(const TasksDev& tk, const MixedPBDev& mp, int b, bool gga, const double* f64c,
+                    const __nv_bfloat16* digc)
+      : d(tk.npts_pad[b], tk.nbe[b]) {
+    double* f64 = const_cast<double*>(f64c);
+    blk = (int64_t)d.np * d.nu128;
+    double* base = f64 + mp.f64_off[b];
+    phi = base;
+    r = base + (gga ? 4 : 1) * blk;
+    sp = r + d.nu128;
+    cz = sp + d.np;
+    phi2 = reinterpret_cast<float2*>(cz + d.nu128);
+    __nv_bfloat16* dg = digc ? const_cast<__nv_bfloat16*>(digc) + mp.dig_off[b] : nullptr;
+    Pd = dg + d.pd();
+    Fd = dg + d.fd();
+    FdT = dg + d.fdt();
+    Zd = dg + d.zd();
+  }
 };
 
-__device__ __forceinline__ PBView view(const TasksDev& tk, const MixedPBDev& mp, int b, bool gga,
-                                       const double* f64c, const __nv_bfloat16* digc) {
-  double* f64 = const_cast<double*>(f64c);
-  __nv_bfloat16* dig = const_cast<__nv_bfloat16*>(digc);
-  PBView v;
-  v.np = tk.npts_pad[b];
-  v.nu = tk.nbe[b];
-  v.nu_pad = tk.nbe_pad[b];
-  v.blk = (int64_t)v.np * v.nu_pad;
-  double* base = f64 + mp.f64_off[b];
-  v.phi = base;
-  v.r = base + (gga ? 4 : 1) * v.blk;
-  v.sp = v.r + v.nu_pad;
-  v.cz = v.sp + v.np;
-  v.phi2 = reinterpret_cast<float2*>(v.cz + v.nu_pad);
-  const int64_t S = kSlices;
-  __nv_bfloat16* d = dig + mp.dig_off[b];
-  v.Pd = d;
-  v.Fd = d + S * v.nu_pad * v.nu_pad;
-  v.FdT = v.Fd + S * v.blk;
-  v.Zd = v.FdT + S * v.blk;
-  return v;
+// Maximum of a 64-bit key over the threads of a CTA that share (tid & 7),
+// i.e. over one of 8 rows handled by the CTA (blockDim.x = 256).
+__device__ __forceinline__ unsigned long long row8_max(unsigned long long m,
+                                                       unsigned long long* red) {
+  m = max(m, __shfl_xor_sync(0xffffffffu, m, 8));
+  m = max(m, __shfl_xor_sync(0xffffffffu, m, 16));
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane < 8) red[w * 8 + lane] = m;
+  __syncthreads();
+  unsigned long long x = 0;
+  for (int k = 0; k < (int)(blockDim.x >> 5); ++k) x = max(x, red[k * 8 + (threadIdx.x & 7)]);
+  __syncthreads();
+  return x;
 }
 
 // ---------------------------------------------------------------- point scales
 __global__ void point_scale_kernel(TasksDev tk, MixedPBDev mp, int b0, double* f64, int gga) {
   const int b = b0 + blockIdx.y;
-  PBView v = view(tk, mp, b, gga, f64, nullptr);
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < v.np; p += gridDim.x * blockDim.x) {
+  PBView v(tk, mp, b, gga, f64, nullptr);
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < v.d.np; p += gridDim.x * blockDim.x) {
     unsigned long long m = 0;
-    for (int mu = 0; mu < v.nu; ++mu) m = max(m, ff::abs_key(v.phi[(int64_t)mu * v.np + p]));
+    for (int mu = 0; mu < v.d.nu; ++mu) m = max(m, ff::abs_key(v.phi[(int64_t)mu * v.d.np + p]));
     v.sp[p] = ff::pow2(ff::scale_exponent(m));
   }
 }
 
 // ---------------------------------------------------------------- phi digits
-// 32 x 32 tiles (mu x p): FdT written along p, Fd written along mu through
-// smem; float-float copies of phi (+ grad) for the density epilogue.
+// FdT (rows mu, K = p): one thread per (mu, 8 points), consecutive threads on
+// consecutive mu.  Fd (rows p, K = mu) and phi2: one thread per (p, 8 basis
+// functions), consecutive threads on consecutive p.
 __global__ void phi_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const double* f64,
                                   __nv_bfloat16* dig, int gga) {
-  __shared__ __nv_bfloat16 t[kSlices][32][34];
   const int b = b0 + blockIdx.y;
-  PBView v = view(tk, mp, b, gga, f64, dig);
-  const int tmu = v.nu_pad / 32, tp = v.np / 32;
+  PBView v(tk, mp, b, gga, f64, dig);
+  const PBDims& d = v.d;
   const int nq = gga ? 4 : 1;
-  for (int tile = blockIdx.x; tile < tmu * tp; tile += gridDim.x) {
-    const int mu0 = (tile / tp) * 32, p0 = (tile % tp) * 32;
-    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
-      const int mu = mu0 + r, p = p0 + threadIdx.x;
-      const int64_t o = (int64_t)mu * v.np + p;
-      const double x = v.phi[o];
-      const int es = exp_of_pow2(v.sp[p]);
-      ff::digits<kSlices>(ff::fixed42(x, es), [&](int i, float d) {
-        const __nv_bfloat16 h = __float2bfloat16_rn(d);
-        v.FdT[i * v.blk + o] = h;
-        t[i][r][threadIdx.x] = h;
-      });
-      for (int q = 0; q < nq; ++q) v.phi2[q * v.blk + o] = ff::split(v.phi[q * v.blk + o]);
-    }
-    __syncthreads();
-    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
-      const int p = p0 + r, mu = mu0 + threadIdx.x;
+  const int stride = gridDim.x * blockDim.x;
+  const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int u = t0; u < d.nu128 * (d.np / 8); u += stride) {
+    const int mu = u % d.nu128, p0 = (u / d.nu128) * 8;
+    double x[8];
+    int es[8];
+    const double2* src = reinterpret_cast<const double2*>(v.phi + (int64_t)mu * d.np + p0);
 #pragma unroll
-      for (int i = 0; i < kSlices; ++i)
-        v.Fd[i * v.blk + (int64_t)p * v.nu_pad + mu] = t[i][threadIdx.x][r];
+    for (int e = 0; e < 4; ++e) {
+      const double2 t = src[e];
+      x[2 * e] = t.x;
+      x[2 * e + 1] = t.y;
     }
-    __syncthreads();
+#pragma unroll
+    for (int e = 0; e < 8; ++e) es[e] = exp_of_pow2(v.sp[p0 + e]);
+    store_digits8(x, es, v.FdT + oz_offset(0, mu, p0, kMTile, d.np), kMTile * kBK);
   }
-}
-
-// Maximum of a 64-bit key over the CTA (blockDim.x a multiple of 32, <= 1024).
-__device__ __forceinline__ unsigned long long block_max(unsigned long long m,
-                                                        unsigned long long* red) {
-  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    unsigned long long x = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0ULL;
-    for (int o = 16; o > 0; o >>= 1) x = max(x, __shfl_xor_sync(0xffffffffu, x, o));
-    if (threadIdx.x == 0) red[0] = x;
+  for (int u = t0; u < d.np * (d.nu128 / 8); u += stride) {
+    const int p = u % d.np, mu0 = (u / d.np) * 8;
+    for (int q = 0; q < nq; ++q) {
+      double x[8];
+#pragma unroll
+      for (int e = 0; e < 8; ++e) x[e] = v.phi[q * v.blk + (int64_t)(mu0 + e) * d.np + p];
+      float4* dst = reinterpret_cast<float4*>(v.phi2 + q * v.blk + (int64_t)p * d.nu128 + mu0);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const float2 a = ff::split(x[2 * e]), c = ff::split(x[2 * e + 1]);
+        dst[e] = make_float4(a.x, a.y, c.x, c.y);
+      }
+      if (q == 0 && mu0 < d.nu16) {
+        int es[8];
+        const int e0 = exp_of_pow2(v.sp[p]);
+#pragma unroll
+        for (int e = 0; e < 8; ++e) es[e] = e0;
+        store_digits8(x, es, v.Fd + oz_offset(0, p, mu0, kNTile, d.nu16), kNTile * kBK);
+      }
+    }
   }
-  __syncthreads();
-  return red[0];
 }
 
 // ---------------------------------------------------------------- P digits
-// One CTA per (row nu, block): gathers P[U_nu, U_mu], row scale, digits.
-__global__ void p_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const double* __restrict__ P,
-                                int nbf, double* f64, __nv_bfloat16* dig, int gga) {
-  __shared__ unsigned long long red[32];
-  const int b = b0 + blockIdx.y;
-  PBView v = view(tk, mp, b, gga, f64, dig);
-  const int row = blockIdx.x;
-  if (row >= v.nu_pad) return;
-  const int* bf = tk.bf_list + tk.bf_off[b];
-  const int gr = bf[row];
+// Row scales of the whole density matrix, once per evaluation: rs[i] is the
+// power of two above max_j |P[i][j]| (one warp per row).
+__global__ void p_row_scales_kernel(const double* __restrict__ P, int nbf, double* __restrict__ rs) {
+  const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (row >= nbf) return;
   unsigned long long m = 0;
-  if (gr >= 0)
-    for (int mu = threadIdx.x; mu < v.nu; mu += blockDim.x) {
-      const int gc = bf[mu];
-      if (gc >= 0) m = max(m, ff::abs_key(P[(int64_t)gr * nbf + gc]));
+  for (int c = lane; c < nbf; c += 32) m = max(m, ff::abs_key(P[(int64_t)row * nbf + c]));
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (lane == 0) rs[row] = ff::pow2(ff::scale_exponent(m));
+}
+
+// Pd (rows nu, K = mu) in one pass.  A warp owns 8 rows: it loads them 32
+// columns at a time, one coalesced row load per instruction (P[U_nu, U_mu]
+// is contiguous along a shell), transposes through shared memory so that lane
+// (row l & 7, column group l >> 3) holds 8 consecutive entries of one row,
+// and splits them with the row's global scale r[nu] = rs[row of nu].  One
+// store instruction then writes four whole 128-byte core matrices of a plane.
+__global__ void p_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const double* __restrict__ P,
+                                const double* __restrict__ rs, int nbf, double* f64,
+                                __nv_bfloat16* dig, int gga) {
+  __shared__ double tile[8][8][33];
+  const int b = b0 + blockIdx.y;
+  PBView v(tk, mp, b, gga, f64, dig);
+  const PBDims& d = v.d;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int row0 = (blockIdx.x * 8 + warp) * 8;
+  if (row0 >= d.nu128) return;
+  const int* bf = tk.bf_list + tk.bf_off[b];
+  const int r = lane & 7, j = lane >> 3;
+  const int gmy = bf[row0 + r];
+  const double rr = gmy >= 0 ? rs[gmy] : ff::pow2(-1022);
+  if (j == 0) v.r[row0 + r] = rr;
+  int es[8];
+  {
+    const int e0 = exp_of_pow2(rr);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) es[e] = e0;
+  }
+  double(*t)[33] = tile[warp];
+  for (int c0 = 0; c0 < d.nu16; c0 += 32) {
+    const int mu = c0 + lane;
+    const int gc = mu < d.nu ? bf[mu] : -1;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int gr = bf[row0 + q];
+      t[q][lane] = (gr >= 0 && gc >= 0) ? P[(int64_t)gr * nbf + gc] : 0.;
     }
-  const int es = ff::scale_exponent(block_max(m, red));
-  if (threadIdx.x == 0) v.r[row] = ff::pow2(es);
-  const int64_t ps = (int64_t)v.nu_pad * v.nu_pad;
-  for (int mu = threadIdx.x; mu < v.nu_pad; mu += blockDim.x) {
-    const int gc = mu < v.nu ? bf[mu] : -1;
-    const double x = (gr >= 0 && gc >= 0) ? P[(int64_t)gr * nbf + gc] : 0.;
-    write_digits(x, es, v.Pd + (int64_t)row * v.nu_pad + mu, ps);
+    __syncwarp();
+    if (c0 + 8 * j < d.nu16) {
+      double x[8];
+#pragma unroll
+      for (int e = 0; e < 8; ++e) x[e] = t[r][8 * j + e];
+      store_digits8(x, es, v.Pd + oz_offset(0, row0 + r, c0 + 8 * j, kMTile, d.nu16),
+                    kMTile * kBK);
+    }
+    __syncwarp();
   }
 }
 
 // ---------------------------------------------------------------- Z digits
 // Zt[nu][p] = sp[p] (zc.x phi + zc.y dphi_x + zc.z dphi_y + zc.w dphi_z),
-// column scale cz[nu] over the block's points, digits Zd[s][nu][p].
+// column scale cz[nu] over the block's points, digits Zd (rows nu, K = p).
+// One CTA per 8 rows nu; thread (row tid & 7, point group tid >> 3).
 __global__ void z_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const double4* __restrict__ zc,
                                 double* f64, __nv_bfloat16* dig, int gga) {
-  __shared__ unsigned long long red[32];
+  __shared__ unsigned long long red[64];
   const int b = b0 + blockIdx.y;
-  PBView v = view(tk, mp, b, gga, f64, dig);
-  const int row = blockIdx.x;
-  if (row >= v.nu_pad) return;
+  PBView v(tk, mp, b, gga, f64, dig);
+  const PBDims& d = v.d;
+  if (blockIdx.x * 8 >= d.nu64) return;
+  const int row = blockIdx.x * 8 + (threadIdx.x & 7);
+  const int ng = d.np / 8, step = blockDim.x / 8;
   const double4* z = zc + tk.pt_off[b];
-  const double* f = v.phi + (int64_t)row * v.np;
+  const double* f = v.phi + (int64_t)row * d.np;
   auto zval = [&](int p) {
     const double4 c = z[p];
     double val = c.x * f[p];
@@ -171,11 +230,20 @@ __global__ void z_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const double
     return v.sp[p] * val;
   };
   unsigned long long m = 0;
-  for (int p = threadIdx.x; p < v.np; p += blockDim.x) m = max(m, ff::abs_key(zval(p)));
-  const int es = ff::scale_exponent(block_max(m, red));
-  if (threadIdx.x == 0) v.cz[row] = ff::pow2(es);
-  for (int p = threadIdx.x; p < v.np; p += blockDim.x)
-    write_digits(zval(p), es, v.Zd + (int64_t)row * v.np + p, v.blk);
+  for (int g = threadIdx.x >> 3; g < ng; g += step)
+    for (int e = 0; e < 8; ++e) m = max(m, ff::abs_key(zval(g * 8 + e)));
+  const int es_row = ff::scale_exponent(row8_max(m, red));
+  if (threadIdx.x < 8) v.cz[row] = ff::pow2(es_row);
+  for (int g = threadIdx.x >> 3; g < ng; g += step) {
+    double x[8];
+    int es[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      x[e] = zval(g * 8 + e);
+      es[e] = es_row;
+    }
+    store_digits8(x, es, v.Zd + oz_offset(0, row, g * 8, kNTile, d.np), kNTile * kBK);
+  }
 }
 
 // ---------------------------------------------------------------- functional
@@ -223,15 +291,22 @@ void launch_point_scales(const TasksDev& tk, const MixedPBDev& mp, int b0, int b
 void launch_phi_digits(const TasksDev& tk, const MixedPBDev& mp, int b0, int b1, bool gga,
                        const double* f64, __nv_bfloat16* dig, cudaStream_t s) {
   if (b1 <= b0) return;
-  phi_digits_kernel<<<dim3(128, b1 - b0), dim3(32, 8), 0, s>>>(tk, mp, b0, f64, dig, gga);
+  phi_digits_kernel<<<dim3(64, b1 - b0), 256, 0, s>>>(tk, mp, b0, f64, dig, gga);
+  GB300_CUDA(cudaGetLastError());
+}
+
+void launch_p_row_scales(const double* P, int nbf, double* rs, cudaStream_t s) {
+  if (nbf <= 0) return;
+  p_row_scales_kernel<<<(nbf + 7) / 8, 256, 0, s>>>(P, nbf, rs);
   GB300_CUDA(cudaGetLastError());
 }
 
 void launch_p_digits(const TasksDev& tk, const MixedPBDev& mp, int b0, int b1, int max_nu_pad,
-                     bool gga, const double* P, int nbf, double* f64, __nv_bfloat16* dig,
-                     cudaStream_t s) {
+                     bool gga, const double* P, const double* rs, int nbf, double* f64,
+                     __nv_bfloat16* dig, cudaStream_t s) {
   if (b1 <= b0) return;
-  p_digits_kernel<<<dim3(max_nu_pad, b1 - b0), 256, 0, s>>>(tk, mp, b0, P, nbf, f64, dig, gga);
+  p_digits_kernel<<<dim3(max_nu_pad / 64, b1 - b0), 256, 0, s>>>(tk, mp, b0, P, rs, nbf, f64, dig,
+                                                                  gga);
   GB300_CUDA(cudaGetLastError());
 }
 
@@ -239,7 +314,8 @@ void launch_z_digits(const TasksDev& tk, const MixedPBDev& mp, int b0, int b1, i
                      bool gga, const double4* zcoef, double* f64, __nv_bfloat16* dig,
                      cudaStream_t s) {
   if (b1 <= b0) return;
-  z_digits_kernel<<<dim3(max_nu_pad, b1 - b0), 128, 0, s>>>(tk, mp, b0, zcoef, f64, dig, gga);
+  z_digits_kernel<<<dim3(max_nu_pad / 8, b1 - b0), 256, 0, s>>>(tk, mp, b0, zcoef, f64, dig,
+                                                                 gga);
   GB300_CUDA(cudaGetLastError());
 }
 

@@ -1,15 +1,23 @@
 // Mixed-precision path: split-mantissa FP64 emulation of the two contractions
 // on BF16 tensor cores (tcgen05.mma, FP32 accumulation in TMEM).
 //
-// Every FP64 operand x is scaled by a power of two 2^e (per row of P, per grid
-// point of phi, per basis column of Z) so that |x| <= 1 and split into
+// Every FP64 operand x is scaled by a power of two 2^e (per row of the whole
+// density matrix, per grid point of phi, per basis column of Z) so that |x| <= 1 and split into
 // kSlices signed digits of 7 bits:  x = 2^e sum_i d_i 2^(-7 i), |d_1| <= 128,
 // |d_i| <= 64 (i > 1).  Digit i is stored in BF16 as d_i 2^(-7 (i - 1)), which
 // is exact.  A product is the sum over slice pairs (i, j) with i + j <= kLevels
-// of BF16 GEMMs; pairs of equal i + j share one TMEM accumulator so each of the
-// four leading levels is an exact integer sum in FP32 (the K extent of one GEMM
-// is at most 512: 512 * 2^15 < 2^24); the remaining pairs (relative weight
-// below 2^-28) share a fifth accumulator.  The epilogue adds the levels in FP64.
+// of BF16 GEMMs; pairs of equal i + j share one TMEM accumulator, so each of
+// the three leading levels is an exact integer sum in FP32 (the K extent of
+// one GEMM is at most 512: 512 * 3 * 2^13 < 2^24).  The remaining pairs
+// (relative weight 2^-21 and below) share a fourth accumulator, whose FP32
+// rounding stays below 2^-44 of the result.  The epilogue adds the levels in
+// float-float arithmetic.
+//
+// GEMM operands live in HBM already in the tensor core's shared-memory image:
+// tiles of TR rows (128 for the M operand, 64 for the N operand) by kBK
+// columns of K, all kSlices digit planes of one tile adjacent, each plane in
+// the K-major no-swizzle layout of 8-row x 16-byte core matrices (oz_offset).
+// One pipeline stage of the GEMM kernel is then two contiguous bulk copies.
 #pragma once
 #include <functional>
 #include <vector>
@@ -24,12 +32,43 @@ namespace gb300 {
 constexpr int kSlices = 6;      // digits per operand
 constexpr int kLevels = 7;      // keep pairs with i + j <= kLevels
 constexpr int kMaxK = 512;      // K extent of one tensor-core GEMM (exactness bound)
-constexpr int kMTile = 128;     // rows of a GEMM tile (basis functions)
-constexpr int kNTile = 64;      // columns of a GEMM tile
+constexpr int kMTile = 128;     // rows of a GEMM tile (M operand)
+constexpr int kNTile = 64;      // columns of a GEMM tile (N operand rows)
+constexpr int kBK = 16;         // K extent of one operand tile (one MMA)
 constexpr int kPBMaxPts = 512;  // points per point block
 
-// Point blocks (merged tasks of one atom) reuse TasksDev; these extra arrays
-// give the per-point member task and the member x shell activity mask.
+__host__ __device__ constexpr int oz_round(int x, int m) { return (x + m - 1) / m * m; }
+
+// Element offset of digit plane s of entry (r, k) of an operand stored as
+// tiles of TR rows; kpad = padded K extent (a multiple of kBK).
+__host__ __device__ inline int64_t oz_offset(int s, int r, int k, int TR, int kpad) {
+  const int64_t chunk = ((int64_t)(r / TR) * (kpad / kBK) + k / kBK) * kSlices + s;
+  const int rr = r % TR, kk = k % kBK;
+  return chunk * TR * kBK + ((rr >> 3) * (kBK / 8) + (kk >> 3)) * 64 + (rr & 7) * 8 + (kk & 7);
+}
+
+// Padded extents of one point block: np points (multiple of kNTile), nu basis
+// functions in the union.
+struct PBDims {
+  int np, nu, nu16, nu64, nu128;
+  __host__ __device__ PBDims(int np_, int nu_)
+      : np(np_), nu(nu_), nu16(oz_round(nu_, kBK)), nu64(oz_round(nu_, kNTile)),
+        nu128(oz_round(nu_, kMTile)) {}
+  // digit operands (bf16 element offsets within the block's region)
+  //   Pd  [nu128 rows, TR 128] x [K = mu, nu16]     density GEMM, M operand
+  //   Fd  [np rows,    TR  64] x [K = mu, nu16]     density GEMM, N operand
+  //   FdT [nu128 rows, TR 128] x [K = p,  np]       VXC GEMM, M operand
+  //   Zd  [nu64 rows,  TR  64] x [K = p,  np]       VXC GEMM, N operand
+  __host__ __device__ int64_t pd() const { return 0; }
+  __host__ __device__ int64_t fd() const { return (int64_t)kSlices * nu128 * nu16; }
+  __host__ __device__ int64_t fdt() const { return fd() + (int64_t)kSlices * np * nu16; }
+  __host__ __device__ int64_t zd() const { return fdt() + (int64_t)kSlices * nu128 * np; }
+  __host__ __device__ int64_t dig_elems() const { return zd() + (int64_t)kSlices * nu64 * np; }
+};
+
+// Point blocks (merged tasks of one atom) reuse TasksDev (npts_pad = np,
+// nbe = nu, nbe_pad = nu128); these extra arrays give the per-point member
+// task and the member x shell activity mask.
 struct PBMaskDev {
   const int* member;        // per padded point: member task index within its block
   const int64_t* mask_off;  // per block: offset into mask
@@ -38,14 +77,22 @@ struct PBMaskDev {
 
 // Per point-block workspace offsets (batch relative).
 struct MixedPBDev {
-  const int64_t* f64_off;   // doubles: phi (+ grad) blocks, then r[nu_pad], sp[np], cz[nu_pad]
-  const int64_t* dig_off;   // bf16 elements: Pd, Fd, FdT, Zd
+  const int64_t* f64_off;   // doubles: phi (+ grad) blocks, r, sp, cz, phi2 (xc_mixed.cu)
+  const int64_t* dig_off;   // bf16 elements: Pd, Fd, FdT, Zd (PBDims)
 };
 
 // One tensor-core GEMM tile: output rows [m0, m0+128) x cols [n0, n0+64),
 // K range [k0, k1) of point block pb.
 struct OzItem {
   int pb, m0, n0, k0, k1;
+};
+
+// Work list of one persistent GEMM launch: CTA c processes
+// items[cta_off[c] .. cta_off[c + 1]) in order.
+struct OzSchedule {
+  const OzItem* items;
+  const int* cta_off;
+  int ncta;
 };
 
 void launch_collocation_masked(const ShellsDev& sh, const TasksDev& tk, const PBMaskDev& mk,
@@ -57,9 +104,11 @@ void launch_point_scales(const TasksDev& tk, const MixedPBDev& mp, int b0, int b
                          double* f64, cudaStream_t s);
 void launch_phi_digits(const TasksDev& tk, const MixedPBDev& mp, int b0, int b1, bool gga,
                        const double* f64, __nv_bfloat16* dig, cudaStream_t s);
+// rs[i]: power of two above max_j |P[i][j]| (launch_p_row_scales, once per call)
+void launch_p_row_scales(const double* P, int nbf, double* rs, cudaStream_t s);
 void launch_p_digits(const TasksDev& tk, const MixedPBDev& mp, int b0, int b1, int max_nu_pad,
-                     bool gga, const double* P, int nbf, double* f64, __nv_bfloat16* dig,
-                     cudaStream_t s);
+                     bool gga, const double* P, const double* rs, int nbf, double* f64,
+                     __nv_bfloat16* dig, cudaStream_t s);
 void launch_z_digits(const TasksDev& tk, const MixedPBDev& mp, int b0, int b1, int max_nu_pad,
                      bool gga, const double4* zcoef, double* f64, __nv_bfloat16* dig,
                      cudaStream_t s);
@@ -70,25 +119,30 @@ void launch_functional(int64_t g0, int64_t g1, const double* w, const double* rh
                        cudaStream_t s);
 
 // Tensor-core GEMMs.  err: device int set non-zero when a bounded wait expired.
-void launch_ozaki_x(const TasksDev& tk, const MixedPBDev& mp, const OzItem* items, int nitems,
+void launch_ozaki_x(const TasksDev& tk, const MixedPBDev& mp, const OzSchedule& sched,
                     const double* f64, const __nv_bfloat16* dig, bool gga, double* rho4,
                     int* err, cudaStream_t s);
-void launch_ozaki_v(const TasksDev& tk, const MixedPBDev& mp, const OzItem* items, int nitems,
+void launch_ozaki_v(const TasksDev& tk, const MixedPBDev& mp, const OzSchedule& sched,
                     const double* f64, const __nv_bfloat16* dig, bool gga, double* A, int nbf,
                     int* err, cudaStream_t s);
+
+// Host: order items[begin, end) into per-CTA lists for a persistent launch on
+// `nsm` CTAs (each tile, in list order, onto the least loaded CTA); appends
+// ncta + 1 absolute offsets to cta_off and returns ncta.
+int ozaki_schedule(std::vector<OzItem>& items, size_t begin, size_t end, int nsm,
+                   std::vector<int>& cta_off);
 
 size_t ozaki_smem_bytes();
 // Tensor-core GEMM self-test (n x n output, K = k); worst relative error.
 double ozaki_selftest(int n, int k);
 
 // Host helpers: workspace sizes of one point block.  The FP64 region holds
-// phi (+ grad) in FP64, the scales r[nu_pad], sp[np], cz[nu_pad], then the same
-// phi (+ grad) as float-float pairs (float2, one double's worth each).
-inline int64_t mixed_f64_doubles(int np, int nu_pad, bool gga) {
-  return 2LL * (gga ? 4 : 1) * np * nu_pad + 2 * nu_pad + np;
+// phi (+ grad) [q][mu][p] in FP64 (nu128 rows), the scales r[nu128], sp[np],
+// cz[nu128], then phi (+ grad) transposed, [q][p][mu], as float-float pairs
+// (float2, one double's worth each).
+inline int64_t mixed_f64_doubles(int np, int nu128, bool gga) {
+  return 2LL * (gga ? 4 : 1) * np * nu128 + 2 * nu128 + np;
 }
-inline int64_t mixed_dig_elems(int np, int nu_pad) {
-  return (int64_t)kSlices * ((int64_t)nu_pad * nu_pad + 3LL * np * nu_pad);
-}
+inline int64_t mixed_dig_elems(int np, int nu) { return PBDims(np, nu).dig_elems(); }
 
 }  // namespace gb300
