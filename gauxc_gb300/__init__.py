@@ -57,7 +57,7 @@ def set_device(dev):
     _call(_L.gauxc_gb300_set_device, int(dev))
 
 
-def tensor_core_selftest(n=256, k=512):
+def tensor_core_selftest(n=256, k=256):
     """Worst relative error of the tensor-core emulated-FP64 GEMM on random data."""
     return float(_call(_L.gauxc_gb300_tensor_core_selftest, int(n), int(k)))
 

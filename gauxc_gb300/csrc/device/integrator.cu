@@ -356,7 +356,7 @@ void DeviceIntegrator::build(const LoadBalancer& lb) {
 
 // Padded tensor-core work of one point block: density GEMM (M = basis rows
 // padded to kMTile, N = points padded to kNTile, K = basis padded to kBK)
-// plus VXC GEMM (M = basis to kMTile, N = basis to kNTile, K = points).
+// plus the symmetric VXC GEMM (about half the M x N basis tiles, K = 2 points).
 static double pb_cost(int npts, int nu) {
   const double np = (double)round_up(npts, kNTile);
   const double m = (double)round_up(nu, kMTile), n = (double)round_up(nu, kNTile),
@@ -511,7 +511,7 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
     mbatches_.push_back(cur);
   };
   for (int i = 0; i < npb; ++i) {
-    const double nf = (double)mixed_f64_doubles(npts_pad[i], nu_pad[i], gga_) * 8.;
+    const double nf = (double)mixed_f64_doubles(npts_pad[i], nu[i], gga_) * 8.;
     const double nd = (double)mixed_dig_elems(npts_pad[i], nu[i]) * 2.;
     if (nf + nd > budget) throw error("insufficient device memory for one point block");
     if (f64_used + dig_used + nf + nd > budget && i > cur.b0) {
@@ -533,8 +533,10 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
       for (int n0 = 0; n0 < d.np; n0 += kNTile)
         for (int k0 = 0; k0 < d.nu16; k0 += kMaxK)
           xi.push_back(OzItem{i, m0, n0, k0, std::min(k0 + kMaxK, d.nu16)});
+    // symmetric VXC: tiles reaching the upper triangle, K = phi | Z
     for (int m0 = 0; m0 < d.nu128; m0 += kMTile)
-      for (int n0 = 0; n0 < d.nu64; n0 += kNTile) vi.push_back(OzItem{i, m0, n0, 0, d.np});
+      for (int n0 = 0; n0 < d.nu64; n0 += kNTile)
+        if (m0 < n0 + kNTile) vi.push_back(OzItem{i, m0, n0, 0, 2 * d.np});
   }
   if (npb > 0) close_batch(npb);
   {

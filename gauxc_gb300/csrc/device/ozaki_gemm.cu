@@ -7,8 +7,10 @@
 //    tile's 128 basis rows (TMEM lanes) run as warp reduce-scatters in
 //    float-float arithmetic and each warp adds its per-point partials to
 //    rho4.  rho is linear in X, so K chunks never need to be summed in X.
-//  V tile (VXC): D[mu, nu] = sum_p FdT[mu, p] Zd[nu, p];
-//    A[mu, nu] += 2^-14 * D * cz_nu, scattered with coalesced FP64 atomics.
+//  V tile (VXC): D[mu, nu] = sum_k Va[mu, k] Vb[nu, k] over K = 2 np, i.e.
+//    (phi^T Z + Z^T phi)[mu, nu] / cz; only tiles reaching the upper triangle
+//    run, and A[mu, nu] += 2^-14 cz D for mu < nu (half of it for mu = nu),
+//    scattered with coalesced FP64 atomics.
 //
 // Persistent, warp-specialised CTAs (one per SM), each walking its own list
 // of tiles:
@@ -156,10 +158,10 @@ __device__ __forceinline__ void operands(const OzItem& it, const TasksDev& tk,
   const int b = it.pb;
   const PBDims d(tk.npts_pad[b], tk.nbe[b]);
   const __nv_bfloat16* base = dig + mp.dig_off[b];
-  const int64_t nkb = (EPI == EPI_X ? d.nu16 : d.np) / kBK;
-  A = base + (EPI == EPI_X ? d.pd() : d.fdt()) +
+  const int64_t nkb = (EPI == EPI_X ? d.nu16 : 2 * d.np) / kBK;
+  A = base + (EPI == EPI_X ? d.pd() : d.va()) +
       (int64_t)(it.m0 / kMTile) * nkb * (kSlices * kMTile * kBK);
-  B = base + (EPI == EPI_X ? d.fd() : d.zd()) +
+  B = base + (EPI == EPI_X ? d.fd() : d.vb()) +
       (int64_t)(it.n0 / kNTile) * nkb * (kSlices * kNTile * kBK);
 }
 
@@ -284,14 +286,14 @@ __global__ void __launch_bounds__(kThreads, 1)
       umma::fence_after_sync();
       const int b = it.pb;
       const PBDims d(tk.npts_pad[b], tk.nbe[b]);
-      const int64_t blk = (int64_t)d.np * d.nu128;
+      const PBF64 o(d, nq);
+      const int64_t blk = o.blk;
       const double* base = f64 + mp.f64_off[b];
-      const double* rvec = base + nq * blk;
-      const double* spv = rvec + d.nu128;
-      const double* czv = spv + d.np;
       const uint32_t tb = lane_base + buf * kAccCols;
       if (EPI == EPI_X) {
-        const float2* phi2 = reinterpret_cast<const float2*>(czv + d.nu128);
+        const double* rvec = base + o.r;
+        const double* spv = base + o.sp;
+        const float2* phi2 = reinterpret_cast<const float2*>(base + o.phi2);
         const int nu = it.m0 + row;
         const int er = exp_of_pow2(rvec[nu]);
         const int64_t g0 = tk.pt_off[b] + it.n0;
@@ -328,23 +330,32 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
         }
       } else {
+        // S[i][j] = (phi^T Z + Z^T phi)[i][j] = 2^(ecz - 14) D: the strict
+        // upper triangle (i < j, union indices) goes to A[i][j], the diagonal
+        // as S[i][i] / 2, so that A + A^T is the block's VXC contribution.
         const int* bfl = tk.bf_list + tk.bf_off[b];
+        const int ecz = exp_of_pow2(base[o.cz]);
+        const int i = it.m0 + row;
         for (int c = c0; c < c0 + 2; ++c) {
           float v[4][16];
           umma::tmem_ld16x4(tb + c * 16, tb + kNTile + c * 16, tb + 2 * kNTile + c * 16,
                             tb + 3 * kNTile + c * 16, v);
 #pragma unroll
           for (int n = 0; n < 16; ++n) {
+            const int j = it.n0 + c * 16 + n;
             const float2 t = sum_levels(v[0][n], v[1][n], v[2][n], v[3][n]);
-            const int ecz = exp_of_pow2(czv[it.n0 + c * 16 + n]);
-            red[lane * kEpiStride + n] = ff::to_double(t.x, t.y, ecz - 14);
+            red[lane * kEpiStride + n] =
+                i <= j ? ff::to_double(t.x, t.y, ecz - 14 - (i == j ? 1 : 0)) : 0.;
           }
           __syncwarp();
           const int n = lane & 15;
-          const int gn = bfl[it.n0 + c * 16 + n];
+          const int jn = it.n0 + c * 16 + n;
+          const int gn = bfl[jn];
           for (int r2 = lane >> 4; r2 < 32; r2 += 2) {
-            const int gm = bfl[it.m0 + q4 * 32 + r2];
-            if (gm >= 0 && gn >= 0) atomicAdd(&out[(int64_t)gm * nbf + gn], red[r2 * kEpiStride + n]);
+            const int im = it.m0 + q4 * 32 + r2;
+            const int gm = bfl[im];
+            if (im <= jn && gm >= 0 && gn >= 0)
+              atomicAdd(&out[(int64_t)gm * nbf + gn], red[r2 * kEpiStride + n]);
           }
           __syncwarp();
         }
@@ -415,33 +426,35 @@ int ozaki_schedule(std::vector<OzItem>& items, size_t begin, size_t end, int nsm
   return ncta;
 }
 
-// Self-test of the VXC-tile GEMM: C[mu][nu] = sum_p F[mu][p] Z[nu][p] for
-// seeded random F in (-1, 1) and Z with row scales spanning 2^-20..2^20,
-// digits built on the host in the tiled operand layout, compared against an
-// FP64 product.  Returns the largest |C - C_ref| / max|C_ref row|.
+// Self-test of the symmetric VXC GEMM: S = F Z^T + Z F^T (n x n) over k
+// points for seeded random F in (-1, 1) and Z with row magnitudes spanning
+// 2^-10..2^10 (one power-of-two scale for all of Z), digits built on the host
+// in the tiled operand layout.  The kernel leaves S[i][j] (i < j) and
+// S[i][i] / 2 in A; returns the largest error against an FP64 S relative to
+// max |S|.
 double ozaki_selftest(int n, int k) {
-  if (n % kMTile || k % kNTile || k > kMaxK) throw std::runtime_error("selftest sizes");
+  if (n % kMTile || k % kNTile || 2 * k > kMaxK) throw std::runtime_error("selftest sizes");
   const PBDims d(k, n);
-  const int np = k;
-  const int64_t blk = (int64_t)np * d.nu128;
+  const int np = k, k2 = 2 * k;
+  const PBF64 o(d, 1);
   uint64_t st = 12345;
   auto rnd = [&]() {
     st = st * 6364136223846793005ULL + 1442695040888963407ULL;
     return ((st >> 11) * (1.0 / 9007199254740992.0)) * 2.0 - 1.0;
   };
-  std::vector<double> F(blk), Z(blk), cz(d.nu128);
+  std::vector<double> F((size_t)n * np), Z((size_t)n * np);
   for (auto& x : F) x = rnd() * 0.999;
+  double zmax = 0.;
   for (int r = 0; r < n; ++r) {
-    const double sc = std::ldexp(1.0, (int)(rnd() * 20));
-    double m = 0.;
+    const double sc = std::ldexp(1.0, (int)(rnd() * 10));
     for (int p = 0; p < np; ++p) {
-      Z[(int64_t)r * np + p] = rnd() * sc;
-      m = std::max(m, std::fabs(Z[(int64_t)r * np + p]));
+      Z[(size_t)r * np + p] = rnd() * sc;
+      zmax = std::max(zmax, std::fabs(Z[(size_t)r * np + p]));
     }
-    int e;
-    std::frexp(m, &e);
-    cz[r] = std::ldexp(1.0, e);
   }
+  int ez;
+  std::frexp(zmax, &ez);
+  const double cz = std::ldexp(1.0, ez);
   std::vector<__nv_bfloat16> dig(d.dig_elems(), __float2bfloat16_rn(0.f));
   auto digits = [&](double x, int64_t at, int64_t plane) {
     double r = x, up = 128.0, keep = 1.0;
@@ -455,17 +468,20 @@ double ozaki_selftest(int n, int k) {
   };
   for (int r = 0; r < n; ++r)
     for (int p = 0; p < np; ++p) {
-      digits(F[(int64_t)r * np + p], d.fdt() + oz_offset(0, r, p, kMTile, np), kMTile * kBK);
-      digits(Z[(int64_t)r * np + p] / cz[r], d.zd() + oz_offset(0, r, p, kNTile, np), kNTile * kBK);
+      const double f = F[(size_t)r * np + p], z = Z[(size_t)r * np + p] / cz;
+      digits(f, d.va() + oz_offset(0, r, p, kMTile, k2), kMTile * kBK);
+      digits(z, d.va() + oz_offset(0, r, np + p, kMTile, k2), kMTile * kBK);
+      digits(z, d.vb() + oz_offset(0, r, p, kNTile, k2), kNTile * kBK);
+      digits(f, d.vb() + oz_offset(0, r, np + p, kNTile, k2), kNTile * kBK);
     }
-  // FP64 region: phi block, r[nu128], sp[np], cz[nu128]
-  std::vector<double> f64(blk + 2 * d.nu128 + np, 0.);
-  for (int r = 0; r < n; ++r) f64[blk + d.nu128 + np + r] = cz[r];
+  std::vector<double> f64(o.total, 0.);
+  for (int r = 0; r < d.nu128; ++r) f64[o.cz + r] = cz;
   std::vector<int> bf(d.nu128);
   for (int i = 0; i < d.nu128; ++i) bf[i] = i;
   std::vector<OzItem> items;
   for (int m0 = 0; m0 < d.nu128; m0 += kMTile)
-    for (int n0 = 0; n0 < d.nu64; n0 += kNTile) items.push_back(OzItem{0, m0, n0, 0, np});
+    for (int n0 = 0; n0 < d.nu64; n0 += kNTile)
+      if (m0 < n0 + kNTile) items.push_back(OzItem{0, m0, n0, 0, k2});
   std::vector<int> cta_off;
   const int ncta = ozaki_schedule(items, 0, items.size(), 148, cta_off);
   int zero_i = 0;
@@ -515,19 +531,22 @@ double ozaki_selftest(int n, int k) {
   cudaFree(derr); cudaFree(doffs); cudaFree(doff); cudaFree(dz); cudaFree(ditems);
   if (herr)
     throw std::runtime_error("selftest: a pipeline wait expired (code " + std::to_string(herr) + ")");
-  double worst = 0.;
-  for (int mu = 0; mu < n; ++mu) {
-    std::vector<double> ref(n);
-    double rmax = 0.;
-    for (int nu = 0; nu < n; ++nu) {
+  std::vector<double> S((size_t)n * n);
+  double smax = 0.;
+  for (int a = 0; a < n; ++a)
+    for (int b = a; b < n; ++b) {
       double acc = 0.;
-      for (int p = 0; p < np; ++p) acc += F[(int64_t)mu * np + p] * Z[(int64_t)nu * np + p];
-      ref[nu] = acc;
-      rmax = std::max(rmax, std::fabs(acc) / cz[nu]);
+      for (int p = 0; p < np; ++p)
+        acc += F[(size_t)a * np + p] * Z[(size_t)b * np + p] + Z[(size_t)a * np + p] * F[(size_t)b * np + p];
+      S[(size_t)a * n + b] = acc;
+      smax = std::max(smax, std::fabs(acc));
     }
-    for (int nu = 0; nu < n; ++nu)
-      worst = std::max(worst, std::fabs(C[(size_t)mu * n + nu] - ref[nu]) / cz[nu] / std::max(rmax, 1e-300));
-  }
+  double worst = 0.;
+  for (int a = 0; a < n; ++a)
+    for (int b = 0; b < n; ++b) {
+      const double ref = b > a ? S[(size_t)a * n + b] : (b == a ? 0.5 * S[(size_t)a * n + a] : 0.);
+      worst = std::max(worst, std::fabs(C[(size_t)a * n + b] - ref) / std::max(smax, 1e-300));
+    }
   return worst;
 }
 

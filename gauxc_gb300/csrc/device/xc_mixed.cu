@@ -2,10 +2,8 @@
 // (slice) generation for P, phi and Z, and the per-point functional.
 //
 // Layouts per point block (PBDims d: np points, nu basis functions):
-//   FP64 region (at f64_off): phi[q][mu][p] (q = value, d/dx, d/dy, d/dz;
-//     nu128 rows) in FP64, r[nu128], sp[np], cz[nu128], then phi2[q][p][mu],
-//     the same values transposed as float-float pairs
-//   digits (bf16, at dig_off): Pd, Fd, FdT, Zd in the tiled operand layout of
+//   FP64 region (at f64_off): PBF64 (phi, scales, phi2)
+//   digits (bf16, at dig_off): Pd, Fd, Va, Vb in the tiled operand layout of
 //     xc_mixed.cuh (oz_offset); every thread writes 8 consecutive K entries
 //     of one row, i.e. one 16-byte row of a core matrix per digit plane
 // Scales are powers of two taken from IEEE exponent bits and digits come from
@@ -48,27 +46,27 @@ __device__ __forceinline__ void store_digits8(const double (&x)[8], const int (&
 
 struct PBView {
   PBDims d;
-  int64_t blk;  // np * nu128
+  PBF64 o;
   const double* phi;
   double *r, *sp, *cz;
-  float2* phi2;  // [q][p][mu]
-  __nv_bfloat16 *Pd, *Fd, *FdT, *Zd;
+  unsigned long long* gkey;  // largest |grad phi| of each point, as abs_key
+  float2* phi2;              // [q][p][mu]
+  __nv_bfloat16 *Pd, *Fd, *Va, *Vb;
   __device__ PBView(const TasksDev& tk, const MixedPBDev& mp, int b, bool gga, const double* f64c,
                     const __nv_bfloat16* digc)
-      : d(tk.npts_pad[b], tk.nbe[b]) {
-    double* f64 = const_cast<double*>(f64c);
-    blk = (int64_t)d.np * d.nu128;
-    double* base = f64 + mp.f64_off[b];
+      : d(tk.npts_pad[b], tk.nbe[b]), o(d, gga ? 4 : 1) {
+    double* base = const_cast<double*>(f64c) + mp.f64_off[b];
     phi = base;
-    r = base + (gga ? 4 : 1) * blk;
-    sp = r + d.nu128;
-    cz = sp + d.np;
-    phi2 = reinterpret_cast<float2*>(cz + d.nu128);
+    r = base + o.r;
+    sp = base + o.sp;
+    gkey = reinterpret_cast<unsigned long long*>(base + o.gp);
+    cz = base + o.cz;
+    phi2 = reinterpret_cast<float2*>(base + o.phi2);
     __nv_bfloat16* dg = digc ? const_cast<__nv_bfloat16*>(digc) + mp.dig_off[b] : nullptr;
     Pd = dg + d.pd();
     Fd = dg + d.fd();
-    FdT = dg + d.fdt();
-    Zd = dg + d.zd();
+    Va = dg + d.va();
+    Vb = dg + d.vb();
   }
 };
 
@@ -88,6 +86,7 @@ __device__ __forceinline__ unsigned long long row8_max(unsigned long long m,
 }
 
 // ---------------------------------------------------------------- point scales
+// sp[p]: power of two above max_mu |phi_mu(p)|; also clears the gradient key.
 __global__ void point_scale_kernel(TasksDev tk, MixedPBDev mp, int b0, double* f64, int gga) {
   const int b = b0 + blockIdx.y;
   PBView v(tk, mp, b, gga, f64, nullptr);
@@ -95,19 +94,22 @@ __global__ void point_scale_kernel(TasksDev tk, MixedPBDev mp, int b0, double* f
     unsigned long long m = 0;
     for (int mu = 0; mu < v.d.nu; ++mu) m = max(m, ff::abs_key(v.phi[(int64_t)mu * v.d.np + p]));
     v.sp[p] = ff::pow2(ff::scale_exponent(m));
+    v.gkey[p] = 0ULL;
   }
 }
 
 // ---------------------------------------------------------------- phi digits
-// FdT (rows mu, K = p): one thread per (mu, 8 points), consecutive threads on
-// consecutive mu.  Fd (rows p, K = mu) and phi2: one thread per (p, 8 basis
-// functions), consecutive threads on consecutive p.
+// Va[mu][p] (K < np) and Vb[mu][np + p] (rows mu < nu64): one thread per
+// (mu, 8 points), consecutive threads on consecutive mu.  Fd (rows p, K = mu)
+// and phi2: thread p of the CTA walks the CTA's share of the basis in groups
+// of 8 (kPBMaxPts <= blockDim.x), tracking the point's largest |grad phi|.
 __global__ void phi_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const double* f64,
                                   __nv_bfloat16* dig, int gga) {
   const int b = b0 + blockIdx.y;
   PBView v(tk, mp, b, gga, f64, dig);
   const PBDims& d = v.d;
   const int nq = gga ? 4 : 1;
+  const int k2 = 2 * d.np;
   const int stride = gridDim.x * blockDim.x;
   const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
   for (int u = t0; u < d.nu128 * (d.np / 8); u += stride) {
@@ -123,15 +125,22 @@ __global__ void phi_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const doub
     }
 #pragma unroll
     for (int e = 0; e < 8; ++e) es[e] = exp_of_pow2(v.sp[p0 + e]);
-    store_digits8(x, es, v.FdT + oz_offset(0, mu, p0, kMTile, d.np), kMTile * kBK);
+    store_digits8(x, es, v.Va + oz_offset(0, mu, p0, kMTile, k2), kMTile * kBK);
+    if (mu < d.nu64) store_digits8(x, es, v.Vb + oz_offset(0, mu, d.np + p0, kNTile, k2), kNTile * kBK);
   }
-  for (int u = t0; u < d.np * (d.nu128 / 8); u += stride) {
-    const int p = u % d.np, mu0 = (u / d.np) * 8;
+  const int p = threadIdx.x;
+  if (p >= d.np) return;
+  const int ng = d.nu128 / 8;
+  const int per = (ng + gridDim.x - 1) / gridDim.x;
+  const int g0 = blockIdx.x * per, g1 = min(ng, g0 + per);
+  unsigned long long gmax = 0;
+  for (int g = g0; g < g1; ++g) {
+    const int mu0 = g * 8;
     for (int q = 0; q < nq; ++q) {
       double x[8];
 #pragma unroll
-      for (int e = 0; e < 8; ++e) x[e] = v.phi[q * v.blk + (int64_t)(mu0 + e) * d.np + p];
-      float4* dst = reinterpret_cast<float4*>(v.phi2 + q * v.blk + (int64_t)p * d.nu128 + mu0);
+      for (int e = 0; e < 8; ++e) x[e] = v.phi[q * v.o.blk + (int64_t)(mu0 + e) * d.np + p];
+      float4* dst = reinterpret_cast<float4*>(v.phi2 + q * v.o.blk + (int64_t)p * d.nu128 + mu0);
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
         const float2 a = ff::split(x[2 * e]), c = ff::split(x[2 * e + 1]);
@@ -144,8 +153,12 @@ __global__ void phi_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const doub
         for (int e = 0; e < 8; ++e) es[e] = e0;
         store_digits8(x, es, v.Fd + oz_offset(0, p, mu0, kNTile, d.nu16), kNTile * kBK);
       }
+      if (q > 0)
+#pragma unroll
+        for (int e = 0; e < 8; ++e) gmax = max(gmax, ff::abs_key(x[e]));
     }
   }
+  if (gga && gmax) atomicMax(v.gkey + p, gmax);
 }
 
 // ---------------------------------------------------------------- P digits
@@ -209,40 +222,61 @@ __global__ void p_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const double
 }
 
 // ---------------------------------------------------------------- Z digits
-// Zt[nu][p] = sp[p] (zc.x phi + zc.y dphi_x + zc.z dphi_y + zc.w dphi_z),
-// column scale cz[nu] over the block's points, digits Zd (rows nu, K = p).
-// One CTA per 8 rows nu; thread (row tid & 7, point group tid >> 3).
+// Zt[nu][p] = sp[p] (zc.x phi + zc.y dphi_x + zc.z dphi_y + zc.w dphi_z) with
+// one scale cz for the whole block: 2^e above the bound
+//   |Zt| <= sp (|zc.x| sp + (|zc.y| + |zc.z| + |zc.w|) max|grad phi|)
+// taken from exponents only.  Digits go to Vb[nu][p] (rows nu < nu64) and
+// Va[nu][np + p] (rows nu < nu128).  One CTA per 8 rows nu; thread (row
+// tid & 7, point group tid >> 3).
 __global__ void z_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const double4* __restrict__ zc,
                                 double* f64, __nv_bfloat16* dig, int gga) {
-  __shared__ unsigned long long red[64];
+  __shared__ int red[32];
   const int b = b0 + blockIdx.y;
   PBView v(tk, mp, b, gga, f64, dig);
   const PBDims& d = v.d;
-  if (blockIdx.x * 8 >= d.nu64) return;
-  const int row = blockIdx.x * 8 + (threadIdx.x & 7);
-  const int ng = d.np / 8, step = blockDim.x / 8;
+  if (blockIdx.x * 8 >= d.nu128) return;
   const double4* z = zc + tk.pt_off[b];
+  // block scale: max over points of the exponent bound
+  int eb = -1000;
+  for (int p = threadIdx.x; p < d.np; p += blockDim.x) {
+    const double4 c = z[p];
+    const int esp = exp_of_pow2(v.sp[p]);
+    int t = ff::scale_exponent(ff::abs_key(c.x)) + esp;
+    if (gga) {
+      const int eg = ff::scale_exponent(v.gkey[p]);
+      t = max(t, ff::scale_exponent(ff::abs_key(c.y)) + eg);
+      t = max(t, ff::scale_exponent(ff::abs_key(c.z)) + eg);
+      t = max(t, ff::scale_exponent(ff::abs_key(c.w)) + eg);
+      t += 2;
+    }
+    eb = max(eb, t + esp);
+  }
+  for (int o = 16; o > 0; o >>= 1) eb = max(eb, __shfl_xor_sync(0xffffffffu, eb, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = eb;
+  __syncthreads();
+  int es_z = -1000;
+  for (int k = 0; k < (int)(blockDim.x >> 5); ++k) es_z = max(es_z, red[k]);
+  es_z = min(max(es_z, -1000), 1000);
+  const int row = blockIdx.x * 8 + (threadIdx.x & 7);
+  if (threadIdx.x < 8) v.cz[row] = ff::pow2(es_z);
+  const int ng = d.np / 8, step = blockDim.x / 8;
+  const int k2 = 2 * d.np;
   const double* f = v.phi + (int64_t)row * d.np;
   auto zval = [&](int p) {
     const double4 c = z[p];
     double val = c.x * f[p];
-    if (gga) val += c.y * f[p + v.blk] + c.z * f[p + 2 * v.blk] + c.w * f[p + 3 * v.blk];
+    if (gga) val += c.y * f[p + v.o.blk] + c.z * f[p + 2 * v.o.blk] + c.w * f[p + 3 * v.o.blk];
     return v.sp[p] * val;
   };
-  unsigned long long m = 0;
-  for (int g = threadIdx.x >> 3; g < ng; g += step)
-    for (int e = 0; e < 8; ++e) m = max(m, ff::abs_key(zval(g * 8 + e)));
-  const int es_row = ff::scale_exponent(row8_max(m, red));
-  if (threadIdx.x < 8) v.cz[row] = ff::pow2(es_row);
+  int es[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) es[e] = es_z;
   for (int g = threadIdx.x >> 3; g < ng; g += step) {
     double x[8];
-    int es[8];
 #pragma unroll
-    for (int e = 0; e < 8; ++e) {
-      x[e] = zval(g * 8 + e);
-      es[e] = es_row;
-    }
-    store_digits8(x, es, v.Zd + oz_offset(0, row, g * 8, kNTile, d.np), kNTile * kBK);
+    for (int e = 0; e < 8; ++e) x[e] = zval(g * 8 + e);
+    store_digits8(x, es, v.Va + oz_offset(0, row, d.np + g * 8, kMTile, k2), kMTile * kBK);
+    if (row < d.nu64) store_digits8(x, es, v.Vb + oz_offset(0, row, g * 8, kNTile, k2), kNTile * kBK);
   }
 }
 

@@ -2,7 +2,7 @@
 // on BF16 tensor cores (tcgen05.mma, FP32 accumulation in TMEM).
 //
 // Every FP64 operand x is scaled by a power of two 2^e (per row of the whole
-// density matrix, per grid point of phi, per basis column of Z) so that |x| <= 1 and split into
+// density matrix, per grid point of phi, per point block for Z) so that |x| <= 1 and split into
 // kSlices signed digits of 7 bits:  x = 2^e sum_i d_i 2^(-7 i), |d_1| <= 128,
 // |d_i| <= 64 (i > 1).  Digit i is stored in BF16 as d_i 2^(-7 (i - 1)), which
 // is exact.  A product is the sum over slice pairs (i, j) with i + j <= kLevels
@@ -35,7 +35,7 @@ constexpr int kMaxK = 512;      // K extent of one tensor-core GEMM (exactness b
 constexpr int kMTile = 128;     // rows of a GEMM tile (M operand)
 constexpr int kNTile = 64;      // columns of a GEMM tile (N operand rows)
 constexpr int kBK = 16;         // K extent of one operand tile (one MMA)
-constexpr int kPBMaxPts = 512;  // points per point block
+constexpr int kPBMaxPts = 256;  // points per point block (2 x 256 = kMaxK for the VXC GEMM)
 
 __host__ __device__ constexpr int oz_round(int x, int m) { return (x + m - 1) / m * m; }
 
@@ -55,15 +55,28 @@ struct PBDims {
       : np(np_), nu(nu_), nu16(oz_round(nu_, kBK)), nu64(oz_round(nu_, kNTile)),
         nu128(oz_round(nu_, kMTile)) {}
   // digit operands (bf16 element offsets within the block's region)
-  //   Pd  [nu128 rows, TR 128] x [K = mu, nu16]     density GEMM, M operand
-  //   Fd  [np rows,    TR  64] x [K = mu, nu16]     density GEMM, N operand
-  //   FdT [nu128 rows, TR 128] x [K = p,  np]       VXC GEMM, M operand
-  //   Zd  [nu64 rows,  TR  64] x [K = p,  np]       VXC GEMM, N operand
+  //   Pd [nu128 rows, TR 128] x [K = mu, nu16]   density GEMM, M operand
+  //   Fd [np rows,    TR  64] x [K = mu, nu16]   density GEMM, N operand
+  //   Va [nu128 rows, TR 128] x [K = 2 np]       VXC GEMM, M operand: phi | Z
+  //   Vb [nu64 rows,  TR  64] x [K = 2 np]       VXC GEMM, N operand: Z | phi
+  // so that Va Vb^T = phi^T Z + Z^T phi, the symmetric VXC contribution.
   __host__ __device__ int64_t pd() const { return 0; }
   __host__ __device__ int64_t fd() const { return (int64_t)kSlices * nu128 * nu16; }
-  __host__ __device__ int64_t fdt() const { return fd() + (int64_t)kSlices * np * nu16; }
-  __host__ __device__ int64_t zd() const { return fdt() + (int64_t)kSlices * nu128 * np; }
-  __host__ __device__ int64_t dig_elems() const { return zd() + (int64_t)kSlices * nu64 * np; }
+  __host__ __device__ int64_t va() const { return fd() + (int64_t)kSlices * np * nu16; }
+  __host__ __device__ int64_t vb() const { return va() + (int64_t)kSlices * nu128 * 2 * np; }
+  __host__ __device__ int64_t dig_elems() const { return vb() + (int64_t)kSlices * nu64 * 2 * np; }
+};
+
+// FP64 region of a point block (offsets in doubles): phi[q][mu][p] (q = value,
+// d/dx, d/dy, d/dz; nu128 rows), r[nu128] (row scales of P), sp[np] (point
+// scales of phi), gp[np] (largest |grad phi| of a point, as an IEEE magnitude
+// key), cz[nu128] (scale of Z, one value per block), then phi2[q][p][mu], the
+// values of phi transposed as float-float pairs (one double's worth each).
+struct PBF64 {
+  int64_t blk, r, sp, gp, cz, phi2, total;
+  __host__ __device__ PBF64(const PBDims& d, int nq)
+      : blk((int64_t)d.np * d.nu128), r(nq * blk), sp(r + d.nu128), gp(sp + d.np),
+        cz(gp + d.np), phi2(cz + d.nu128), total(phi2 + nq * blk) {}
 };
 
 // Point blocks (merged tasks of one atom) reuse TasksDev (npts_pad = np,
@@ -77,8 +90,8 @@ struct PBMaskDev {
 
 // Per point-block workspace offsets (batch relative).
 struct MixedPBDev {
-  const int64_t* f64_off;   // doubles: phi (+ grad) blocks, r, sp, cz, phi2 (xc_mixed.cu)
-  const int64_t* dig_off;   // bf16 elements: Pd, Fd, FdT, Zd (PBDims)
+  const int64_t* f64_off;   // doubles: PBF64 layout
+  const int64_t* dig_off;   // bf16 elements: PBDims layout
 };
 
 // One tensor-core GEMM tile: output rows [m0, m0+128) x cols [n0, n0+64),
@@ -133,15 +146,13 @@ int ozaki_schedule(std::vector<OzItem>& items, size_t begin, size_t end, int nsm
                    std::vector<int>& cta_off);
 
 size_t ozaki_smem_bytes();
-// Tensor-core GEMM self-test (n x n output, K = k); worst relative error.
+// Self-test of the symmetric VXC GEMM (n x n output, k points); worst error
+// relative to the largest output element.
 double ozaki_selftest(int n, int k);
 
-// Host helpers: workspace sizes of one point block.  The FP64 region holds
-// phi (+ grad) [q][mu][p] in FP64 (nu128 rows), the scales r[nu128], sp[np],
-// cz[nu128], then phi (+ grad) transposed, [q][p][mu], as float-float pairs
-// (float2, one double's worth each).
-inline int64_t mixed_f64_doubles(int np, int nu128, bool gga) {
-  return 2LL * (gga ? 4 : 1) * np * nu128 + 2 * nu128 + np;
+// Host helpers: workspace sizes of one point block.
+inline int64_t mixed_f64_doubles(int np, int nu, bool gga) {
+  return PBF64(PBDims(np, nu), gga ? 4 : 1).total;
 }
 inline int64_t mixed_dig_elems(int np, int nu) { return PBDims(np, nu).dig_elems(); }
 

@@ -265,9 +265,10 @@ int gauxc_gb300_integrator_kernel_times(GauXCStatus* status, const GauXCIntegrat
                                         double* out, int nmax);
 /* Measured FP64 FMA throughput of the current device in TFLOP/s (about 50 ms probe). */
 double gauxc_gb300_measure_fp64_peak(GauXCStatus* status);
-/* Self-test of the tensor-core (split-mantissa BF16) GEMM: an n x n product with
-   inner dimension k (n multiple of 128, k multiple of 64, k <= 512) against FP64;
-   returns the worst error relative to the output row scale. */
+/* Self-test of the tensor-core (split-mantissa BF16) VXC GEMM: the symmetric
+   n x n product F Z^T + Z F^T over k points (n multiple of 128, k multiple of
+   64, k <= 256) against FP64; returns the worst error relative to the largest
+   output element. */
 double gauxc_gb300_tensor_core_selftest(GauXCStatus* status, int n, int k);
 /* cudaSetDevice for the calling thread (one process per GPU). */
 void gauxc_gb300_set_device(GauXCStatus* status, int device);
