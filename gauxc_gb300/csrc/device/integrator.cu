@@ -535,7 +535,7 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
           xi.push_back(OzItem{i, m0, n0, k0, std::min(k0 + kMaxK, d.nu16)});
     // symmetric VXC: tiles reaching the upper triangle, K = phi | Z
     for (int m0 = 0; m0 < d.nu128; m0 += kMTile)
-      for (int n0 = 0; n0 < d.nu64; n0 += kNTile)
+      for (int n0 = 0; n0 < d.nun; n0 += kNTile)
         if (m0 < n0 + kNTile) vi.push_back(OzItem{i, m0, n0, 0, 2 * d.np});
   }
   if (npb > 0) close_batch(npb);

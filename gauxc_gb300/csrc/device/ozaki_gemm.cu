@@ -13,18 +13,23 @@
 //    scattered with coalesced FP64 atomics.
 //
 // Persistent, warp-specialised CTAs (one per SM), each walking its own list
-// of tiles:
+// of tiles (128 x 64 outputs):
 //   warp 0    producer: two bulk copies per K block (the operands are stored
 //             in HBM as shared-memory images, xc_mixed.cuh) into a kStages
 //             ring, completion counted on the stage's `full` mbarrier;
-//   warp 1    one lane issues the 21 slice-pair MMAs of a K block and commits
-//             them to the stage's `empty` mbarrier; after a tile's last block
-//             it commits to the TMEM buffer's `tfull` mbarrier;
+//   warp 1    one lane issues the MMAs of a K block and commits them to the
+//             stage's `empty` mbarrier; after a tile's last block it commits
+//             to `tfull`.  Each level i + j (0..5) of the slice-pair
+//             products has its own exact FP32 accumulator of 64 TMEM columns,
+//             placed so that digit plane i of A times adjacent B planes
+//             j0 .. j1 is a single MMA of N = 64 (j1 - j0 + 1) <= 256 writing
+//             levels i + j0 .. i + j1: 8 MMAs per K block instead of 21, so A
+//             is read from shared memory 8 times instead of 21;
 //   warps 2-9 epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31, columns
-//             32 ((w - 2) / 4) .. +31 of each accumulator.  Two TMEM buffers
-//             of four level accumulators (2 x 256 columns) let a tile's
-//             epilogue overlap the next tile's main loop; `tempty` hands a
-//             buffer back.
+//             32 ((w - 2) / 4) .. +31 of each level.  The six levels of a
+//             column are summed into a float-float value right away, TMEM is
+//             handed back (`tempty`) and the rest of the epilogue runs from
+//             registers while the next tile's MMAs proceed.
 // Every mbarrier wait is bounded.  On expiry the CTA records an error code,
 // each role leaves its loop, the producer waits (bounded) for its copies in
 // flight, the MMA lane for its MMAs, and TMEM is released.
@@ -47,23 +52,22 @@ namespace gb300 {
 namespace {
 
 constexpr int kStages = 5;
-constexpr int kEpiWarps = 8;  // two per TMEM lane quarter, each on half the columns
+constexpr int kEpiWarps = 8;  // two per TMEM lane quarter, 32 columns each
 constexpr int kThreads = 64 + 32 * kEpiWarps;
-constexpr int kAccs = 4;
+constexpr int kAccs = kLevels - 1;  // exact level accumulators (i + j = 0..5)
 constexpr int kAPlane = kMTile * kBK * 2;  // bytes of one digit plane of an A tile (4 KB)
 constexpr int kBPlane = kNTile * kBK * 2;  // bytes of one digit plane of a B tile (2 KB)
 constexpr int kABytes = kSlices * kAPlane;
 constexpr int kBBytes = kSlices * kBPlane;
 constexpr int kStageBytes = kABytes + kBBytes;
-constexpr int kAccCols = kAccs * kNTile;  // TMEM columns of one buffer
-constexpr uint32_t kTmemCols = 2 * kAccCols;
+constexpr uint32_t kTmemCols = 512;  // six levels x 64 columns (384) rounded up
 constexpr int kEpiStride = 17;  // padded row of a warp's 32 x 16 transposition tile
 constexpr int kEpiBytes = kEpiWarps * 32 * kEpiStride * 8;
 constexpr int kBarOffset = kStages * kStageBytes + kEpiBytes;
 constexpr uint32_t kWaitLimit = 1u << 22;
-constexpr uint32_t kIdesc = umma::idesc_bf16_f32(kMTile, kNTile);
 static_assert(kBK == 16, "one MMA (K = 16) per operand tile");
-static_assert(kTmemCols <= 512, "TMEM holds 512 columns");
+static_assert(kNTile == 64 && kAccs * kNTile <= (int)kTmemCols, "six levels of 64 columns");
+static_assert(kSlices == 6 && kLevels == 7, "MMA grouping below assumes 6 digits, levels <= 7");
 
 enum { EPI_X = 0, EPI_V = 1 };
 // error codes: which wait expired
@@ -72,8 +76,8 @@ enum { ERR_EMPTY = 1, ERR_TEMPTY = 2, ERR_FULL = 3, ERR_TFULL = 4 };
 struct Bars {
   uint64_t full[kStages];
   uint64_t empty[kStages];
-  uint64_t tfull[2];
-  uint64_t tempty[2];
+  uint64_t tfull;
+  uint64_t tempty;
   uint64_t done;
   uint32_t tmem_slot;
   int fail;
@@ -97,20 +101,26 @@ __device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity) {
   return __all_sync(0xffffffffu, ok);
 }
 
-// The 21 slice-pair MMAs of one K block: pair (i, j) (0-based digits,
-// i + j + 2 <= kLevels) accumulates into level accumulator min(i + j, 3).
+// The MMAs of one K block.  Digit plane i of A times B planes j0..j1 (adjacent
+// in shared memory, so one operand of 64 (j1 - j0 + 1) rows) accumulates into
+// levels i + j0 .. i + j1 (TMEM columns 64 (i + j0) ..), all pairs with
+// i + j <= 5.  On a tile's first block the two plane-0 MMAs, which cover all
+// six levels, overwrite instead of accumulating.
 __device__ __forceinline__ void issue_block(uint32_t d0, uint32_t a0, uint32_t b0, bool acc_prev) {
-#pragma unroll
-  for (int i = 0; i < kSlices; ++i)
-#pragma unroll
-    for (int j = 0; j < kSlices; ++j) {
-      if (i + j + 2 > kLevels) continue;
-      const int acc = i + j < kAccs - 1 ? i + j : kAccs - 1;
-      const bool first = (i == 0) && (j <= kAccs - 1);  // first pair of its accumulator
-      const uint64_t ad = umma::smem_desc(a0 + i * kAPlane, 128, (kBK / 8) * 128);
-      const uint64_t bd = umma::smem_desc(b0 + j * kBPlane, 128, (kBK / 8) * 128);
-      umma::mma_bf16(d0 + acc * kNTile, ad, bd, kIdesc, (acc_prev || !first) ? 1u : 0u);
-    }
+  auto mma = [&](int i, int j0, int nplanes, bool first) {
+    const uint64_t ad = umma::smem_desc(a0 + i * kAPlane, 128, (kBK / 8) * 128);
+    const uint64_t bd = umma::smem_desc(b0 + j0 * kBPlane, 128, (kBK / 8) * 128);
+    const uint32_t idesc = umma::idesc_bf16_f32(kMTile, kNTile * nplanes);
+    umma::mma_bf16(d0 + (i + j0) * kNTile, ad, bd, idesc, (acc_prev || !first) ? 1u : 0u);
+  };
+  mma(0, 0, 4, true);   // levels 0-3
+  mma(0, 4, 2, true);   // levels 4-5
+  mma(1, 0, 4, false);  // levels 1-4
+  mma(1, 4, 1, false);  // level 5
+  mma(2, 0, 4, false);  // levels 2-5
+  mma(3, 0, 3, false);  // levels 3-5
+  mma(4, 0, 2, false);  // levels 4-5
+  mma(5, 0, 1, false);  // level 5
 }
 
 // Sum over the 32 lanes of 16 float-float values per lane (reduce-scatter):
@@ -140,13 +150,27 @@ __device__ __forceinline__ void reduce16(float (&h)[16], float (&l)[16], int lan
   l[0] = t.y;
 }
 
-// Exact float-float sum of the four level accumulators of one column.
-__device__ __forceinline__ float2 sum_levels(float a, float b, float c, float d) {
-  float s, e, s2, e2, s3, e3;
-  ff::two_sum(a, b, s, e);
-  ff::two_sum(s, c, s2, e2);
-  ff::two_sum(s2, d, s3, e3);
-  return make_float2(s3, e + e2 + e3);
+// This thread's lane of TMEM columns [col, col + 16) of the six levels, summed
+// into float-float values.
+__device__ __forceinline__ void drain_levels(uint32_t tb, uint32_t col, float (&hi)[16],
+                                             float (&lo)[16]) {
+  const uint32_t t[6] = {tb + col, tb + kNTile + col, tb + 2 * kNTile + col,
+                         tb + 3 * kNTile + col, tb + 4 * kNTile + col, tb + 5 * kNTile + col};
+  float v[6][16];
+  umma::tmem_ld16x6(t, v);
+#pragma unroll
+  for (int n = 0; n < 16; ++n) {
+    float s = v[0][n], e = 0.f;
+#pragma unroll
+    for (int a = 1; a < 6; ++a) {
+      float u, d;
+      ff::two_sum(s, v[a][n], u, d);
+      s = u;
+      e += d;
+    }
+    hi[n] = s;
+    lo[n] = e;
+  }
 }
 
 // First element of the tile row block holding rows [m0, m0 + TR) of an
@@ -182,10 +206,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       umma::mbar_init(&B->full[s], 1);
       umma::mbar_init(&B->empty[s], 1);
     }
-    for (int s = 0; s < 2; ++s) {
-      umma::mbar_init(&B->tfull[s], 1);
-      umma::mbar_init(&B->tempty[s], kEpiWarps);
-    }
+    umma::mbar_init(&B->tfull, 1);
+    umma::mbar_init(&B->tempty, kEpiWarps);
     umma::mbar_init(&B->done, 1);
     B->fail = 0;
     umma::fence_barrier_init();
@@ -234,13 +256,13 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int ii = beg; ii < end; ++ii, ++li) {
       if (warp_failed(B)) break;
       const OzItem it = sched.items[ii];
-      const int buf = li & 1;
-      if (li >= 2 && !warp_wait(&B->tempty[buf], ((li >> 1) - 1) & 1)) {
+      // the epilogue has drained the previous tile's accumulators
+      if (li >= 1 && !warp_wait(&B->tempty, (li - 1) & 1)) {
         if (lane == 0) set_fail(B, ERR_TEMPTY);
         break;
       }
       umma::fence_after_sync();
-      const uint32_t d0 = tmem + buf * kAccCols;
+      const uint32_t d0 = tmem;
       const int nkb = (it.k1 - it.k0) / kBK;
       bool ok = true;
       for (int kb = 0; kb < nkb; ++kb, ++g) {
@@ -259,7 +281,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         __syncwarp();
       }
       if (!ok) break;
-      if (lane == 0) umma::mma_commit(&B->tfull[buf]);
+      if (lane == 0) umma::mma_commit(&B->tfull);
       __syncwarp();
     }
     // every MMA issued above has completed before TMEM is released
@@ -268,8 +290,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     warp_wait(&B->done, 0);
   } else {
     // ------------------------------------------------------------ epilogue
-    const int q4 = warp & 3;  // TMEM lane quarter this warp may access
-    const int c0 = ((warp - 2) >> 2) * 2;  // first of this warp's two 16-column chunks
+    const int q4 = warp & 3;                   // TMEM lane quarter this warp may access
+    const int c0 = ((warp - 2) >> 2) * 2;      // first of this warp's two 16-column chunks
     const int row = q4 * 32 + lane;
     const uint32_t lane_base = tmem + ((uint32_t)(q4 * 32) << 16);
     double* red = reinterpret_cast<double*>(smem + kStages * kStageBytes) + (warp - 2) * 32 * kEpiStride;
@@ -278,46 +300,58 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int ii = beg; ii < end; ++ii, ++li) {
       if (warp_failed(B)) break;
       const OzItem it = sched.items[ii];
-      const int buf = li & 1;
-      if (!warp_wait(&B->tfull[buf], (li >> 1) & 1)) {
+      // Tile prologue, before the accumulators are ready: metadata, scales
+      // and global indices.
+      const int b = it.pb;
+      const PBDims d(tk.npts_pad[b], tk.nbe[b]);
+      const PBF64 o(d, nq);
+      const double* base = f64 + mp.f64_off[b];
+      const int i = it.m0 + row;               // tile row (basis function nu / mu)
+      const int jl = it.n0 + c0 * 16 + lane;   // this lane's column of the warp's 32
+      int e_row = 0, e_col = 0, gm_l = 0, gn_l = 0, ecz = 0;
+      const float2* phi2 = nullptr;
+      if (EPI == EPI_X) {
+        e_row = exp_of_pow2(base[o.r + i]);
+        e_col = exp_of_pow2(base[o.sp + jl]);
+        phi2 = reinterpret_cast<const float2*>(base + o.phi2);
+      } else {
+        const int* bfl = tk.bf_list + tk.bf_off[b];
+        gm_l = bfl[i];
+        gn_l = bfl[jl];
+        ecz = exp_of_pow2(base[o.cz]);
+      }
+      if (!warp_wait(&B->tfull, li & 1)) {
         if (lane == 0) set_fail(B, ERR_TFULL);
         break;
       }
       umma::fence_after_sync();
-      const int b = it.pb;
-      const PBDims d(tk.npts_pad[b], tk.nbe[b]);
-      const PBF64 o(d, nq);
-      const int64_t blk = o.blk;
-      const double* base = f64 + mp.f64_off[b];
-      const uint32_t tb = lane_base + buf * kAccCols;
+      // levels -> float-float in registers, then TMEM goes back to the MMAs
+      float hi[2][16], lo[2][16];
+      drain_levels(lane_base, c0 * 16, hi[0], lo[0]);
+      drain_levels(lane_base, c0 * 16 + 16, hi[1], lo[1]);
+      umma::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) umma::mbar_arrive(&B->tempty);
       if (EPI == EPI_X) {
-        const double* rvec = base + o.r;
-        const double* spv = base + o.sp;
-        const float2* phi2 = reinterpret_cast<const float2*>(base + o.phi2);
-        const int nu = it.m0 + row;
-        const int er = exp_of_pow2(rvec[nu]);
-        const int64_t g0 = tk.pt_off[b] + it.n0;
-        for (int c = c0; c < c0 + 2; ++c) {
-          float v[4][16];
-          umma::tmem_ld16x4(tb + c * 16, tb + kNTile + c * 16, tb + 2 * kNTile + c * 16,
-                            tb + 3 * kNTile + c * 16, v);
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+          const int c = c0 + k;
+          const int64_t g0 = tk.pt_off[b] + it.n0 + c * 16;
           // X'[nu, p] = 2^(er + esp - 13) D, a power of two times D
-          float hi[16], lo[16];
 #pragma unroll
           for (int n = 0; n < 16; ++n) {
-            const float2 t = sum_levels(v[0][n], v[1][n], v[2][n], v[3][n]);
-            const float sc = ff::pow2f(er + exp_of_pow2(spv[it.n0 + c * 16 + n]) - 13);
-            hi[n] = t.x * sc;
-            lo[n] = t.y * sc;
+            const float sc = ff::pow2f(e_row + __shfl_sync(0xffffffffu, e_col, 16 * k + n) - 13);
+            hi[k][n] *= sc;
+            lo[k][n] *= sc;
           }
           for (int q = 0; q < nq; ++q) {
             float h[16], l[16];
-            const float2* f = phi2 + q * blk + (int64_t)(it.n0 + c * 16) * d.nu128 + nu;
+            const float2* f = phi2 + q * o.blk + (int64_t)(it.n0 + c * 16) * d.nu128 + i;
 #pragma unroll
             for (int n = 0; n < 16; ++n) {
               float2 fv = f[(int64_t)n * d.nu128];
               if (q) fv = make_float2(2.f * fv.x, 2.f * fv.y);
-              const float2 t = ff::mul(make_float2(hi[n], lo[n]), fv);
+              const float2 t = ff::mul(make_float2(hi[k][n], lo[k][n]), fv);
               h[n] = t.x;
               l[n] = t.y;
             }
@@ -325,7 +359,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             if ((lane & 1) == 0) {
               const int n = ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 +
                             ((lane >> 1) & 1);
-              atomicAdd(&out[4 * (g0 + c * 16 + n) + q], ff::to_double(h[0], l[0], 0));
+              atomicAdd(&out[4 * (g0 + n) + q], ff::to_double_fast(h[0], l[0], 0));
             }
           }
         }
@@ -333,36 +367,28 @@ __global__ void __launch_bounds__(kThreads, 1)
         // S[i][j] = (phi^T Z + Z^T phi)[i][j] = 2^(ecz - 14) D: the strict
         // upper triangle (i < j, union indices) goes to A[i][j], the diagonal
         // as S[i][i] / 2, so that A + A^T is the block's VXC contribution.
-        const int* bfl = tk.bf_list + tk.bf_off[b];
-        const int ecz = exp_of_pow2(base[o.cz]);
-        const int i = it.m0 + row;
-        for (int c = c0; c < c0 + 2; ++c) {
-          float v[4][16];
-          umma::tmem_ld16x4(tb + c * 16, tb + kNTile + c * 16, tb + 2 * kNTile + c * 16,
-                            tb + 3 * kNTile + c * 16, v);
 #pragma unroll
-          for (int n = 0; n < 16; ++n) {
-            const int j = it.n0 + c * 16 + n;
-            const float2 t = sum_levels(v[0][n], v[1][n], v[2][n], v[3][n]);
+        for (int k = 0; k < 2; ++k) {
+          const int j0 = it.n0 + (c0 + k) * 16;
+#pragma unroll
+          for (int n = 0; n < 16; ++n)
             red[lane * kEpiStride + n] =
-                i <= j ? ff::to_double(t.x, t.y, ecz - 14 - (i == j ? 1 : 0)) : 0.;
-          }
+                i <= j0 + n ? ff::to_double_fast(hi[k][n], lo[k][n], ecz - 14 - (i == j0 + n ? 1 : 0))
+                            : 0.;
           __syncwarp();
           const int n = lane & 15;
-          const int jn = it.n0 + c * 16 + n;
-          const int gn = bfl[jn];
-          for (int r2 = lane >> 4; r2 < 32; r2 += 2) {
+          const int gn = __shfl_sync(0xffffffffu, gn_l, 16 * k + n);
+#pragma unroll
+          for (int t = 0; t < 16; ++t) {
+            const int r2 = (lane >> 4) + 2 * t;
             const int im = it.m0 + q4 * 32 + r2;
-            const int gm = bfl[im];
-            if (im <= jn && gm >= 0 && gn >= 0)
+            const int gm = __shfl_sync(0xffffffffu, gm_l, r2);
+            if (im <= j0 + n && gm >= 0 && gn >= 0)
               atomicAdd(&out[(int64_t)gm * nbf + gn], red[r2 * kEpiStride + n]);
           }
           __syncwarp();
         }
       }
-      umma::fence_before_sync();
-      __syncwarp();
-      if (lane == 0) umma::mbar_arrive(&B->tempty[buf]);
     }
   }
 
@@ -480,7 +506,7 @@ double ozaki_selftest(int n, int k) {
   for (int i = 0; i < d.nu128; ++i) bf[i] = i;
   std::vector<OzItem> items;
   for (int m0 = 0; m0 < d.nu128; m0 += kMTile)
-    for (int n0 = 0; n0 < d.nu64; n0 += kNTile)
+    for (int n0 = 0; n0 < d.nun; n0 += kNTile)
       if (m0 < n0 + kNTile) items.push_back(OzItem{0, m0, n0, 0, k2});
   std::vector<int> cta_off;
   const int ncta = ozaki_schedule(items, 0, items.size(), 148, cta_off);

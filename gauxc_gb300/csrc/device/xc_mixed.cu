@@ -99,7 +99,7 @@ __global__ void point_scale_kernel(TasksDev tk, MixedPBDev mp, int b0, double* f
 }
 
 // ---------------------------------------------------------------- phi digits
-// Va[mu][p] (K < np) and Vb[mu][np + p] (rows mu < nu64): one thread per
+// Va[mu][p] (K < np) and Vb[mu][np + p] (rows mu < nun): one thread per
 // (mu, 8 points), consecutive threads on consecutive mu.  Fd (rows p, K = mu)
 // and phi2: thread p of the CTA walks the CTA's share of the basis in groups
 // of 8 (kPBMaxPts <= blockDim.x), tracking the point's largest |grad phi|.
@@ -126,7 +126,7 @@ __global__ void phi_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const doub
 #pragma unroll
     for (int e = 0; e < 8; ++e) es[e] = exp_of_pow2(v.sp[p0 + e]);
     store_digits8(x, es, v.Va + oz_offset(0, mu, p0, kMTile, k2), kMTile * kBK);
-    if (mu < d.nu64) store_digits8(x, es, v.Vb + oz_offset(0, mu, d.np + p0, kNTile, k2), kNTile * kBK);
+    if (mu < d.nun) store_digits8(x, es, v.Vb + oz_offset(0, mu, d.np + p0, kNTile, k2), kNTile * kBK);
   }
   const int p = threadIdx.x;
   if (p >= d.np) return;
@@ -225,7 +225,7 @@ __global__ void p_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const double
 // Zt[nu][p] = sp[p] (zc.x phi + zc.y dphi_x + zc.z dphi_y + zc.w dphi_z) with
 // one scale cz for the whole block: 2^e above the bound
 //   |Zt| <= sp (|zc.x| sp + (|zc.y| + |zc.z| + |zc.w|) max|grad phi|)
-// taken from exponents only.  Digits go to Vb[nu][p] (rows nu < nu64) and
+// taken from exponents only.  Digits go to Vb[nu][p] (rows nu < nun) and
 // Va[nu][np + p] (rows nu < nu128).  One CTA per 8 rows nu; thread (row
 // tid & 7, point group tid >> 3).
 __global__ void z_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const double4* __restrict__ zc,
@@ -276,7 +276,7 @@ __global__ void z_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const double
 #pragma unroll
     for (int e = 0; e < 8; ++e) x[e] = zval(g * 8 + e);
     store_digits8(x, es, v.Va + oz_offset(0, row, d.np + g * 8, kMTile, k2), kMTile * kBK);
-    if (row < d.nu64) store_digits8(x, es, v.Vb + oz_offset(0, row, g * 8, kNTile, k2), kNTile * kBK);
+    if (row < d.nun) store_digits8(x, es, v.Vb + oz_offset(0, row, g * 8, kNTile, k2), kNTile * kBK);
   }
 }
 

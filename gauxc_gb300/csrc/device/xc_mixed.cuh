@@ -50,21 +50,21 @@ __host__ __device__ inline int64_t oz_offset(int s, int r, int k, int TR, int kp
 // Padded extents of one point block: np points (multiple of kNTile), nu basis
 // functions in the union.
 struct PBDims {
-  int np, nu, nu16, nu64, nu128;
+  int np, nu, nu16, nun, nu128;
   __host__ __device__ PBDims(int np_, int nu_)
-      : np(np_), nu(nu_), nu16(oz_round(nu_, kBK)), nu64(oz_round(nu_, kNTile)),
+      : np(np_), nu(nu_), nu16(oz_round(nu_, kBK)), nun(oz_round(nu_, kNTile)),
         nu128(oz_round(nu_, kMTile)) {}
   // digit operands (bf16 element offsets within the block's region)
   //   Pd [nu128 rows, TR 128] x [K = mu, nu16]   density GEMM, M operand
   //   Fd [np rows,    TR  64] x [K = mu, nu16]   density GEMM, N operand
   //   Va [nu128 rows, TR 128] x [K = 2 np]       VXC GEMM, M operand: phi | Z
-  //   Vb [nu64 rows,  TR  64] x [K = 2 np]       VXC GEMM, N operand: Z | phi
+  //   Vb [nun rows,   TR  64] x [K = 2 np]       VXC GEMM, N operand: Z | phi
   // so that Va Vb^T = phi^T Z + Z^T phi, the symmetric VXC contribution.
   __host__ __device__ int64_t pd() const { return 0; }
   __host__ __device__ int64_t fd() const { return (int64_t)kSlices * nu128 * nu16; }
   __host__ __device__ int64_t va() const { return fd() + (int64_t)kSlices * np * nu16; }
   __host__ __device__ int64_t vb() const { return va() + (int64_t)kSlices * nu128 * 2 * np; }
-  __host__ __device__ int64_t dig_elems() const { return vb() + (int64_t)kSlices * nu64 * 2 * np; }
+  __host__ __device__ int64_t dig_elems() const { return vb() + (int64_t)kSlices * nun * 2 * np; }
 };
 
 // FP64 region of a point block (offsets in doubles): phi[q][mu][p] (q = value,
