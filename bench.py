@@ -33,6 +33,8 @@ WORKLOADS = {
     0: "1 water, SVWN5, MK 75x302 unpruned, 60 bf",
     1: "32 waters (10 A cube), PBE, MK 99x590 Treutler, 1920 bf, nocc 160",
     2: "96 waters (14 A cube), PBE, MK 75x302 Treutler, 5760 bf, nocc 480",
+    3: "64 clusters of 1-40 waters, half SVWN5 / half PBE, MK 75x302 Treutler, batch 128-1024, "
+       "one CUDA-graph launch per SCF iteration",
     4: "256 waters (20 A cube), PBE, MK 75x302 Treutler, tol 1e-12, 15360 bf, nocc 1280",
     5: "profiling case: 4 waters (6 A cube), PBE, MK 99x590 Treutler, 240 bf",
 }
@@ -201,6 +203,140 @@ def time_cpu(W, basis, lb, P, func, budget_s=15.0, nthreads=0):
         frac = min(1.0, frac * max(2.0, min(8.0, (budget_s / 4) / max(dt, 1e-3))))
 
 
+# ---------------------------------------------------------------------- batched
+def run_batched(args, dist, rank, local, ncores):
+    """The batched workload: every cluster's EXC+VXC in one graph launch."""
+    import gauxc_gb300 as g
+    from gauxc_gb300 import workloads as W
+    g.set_device(local)
+    cfg = W.config(args.config)
+    t0 = time.perf_counter()
+    systems = []
+    for s in cfg["systems"]:
+        mol, basis, mg, lb = W.build_system(s)
+        systems.append((s, mol, basis, mg, lb))
+    t_lb = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    mw = g.MolecularWeightsFactory(g.ExecutionSpace.Device).get_instance()
+    for s, mol, basis, mg, lb in systems:
+        mw.modify_weights(lb)
+    t_w = time.perf_counter() - t0
+
+    def make(lwd):
+        f = g.XCIntegratorFactory(g.ExecutionSpace.Device, "Replicated", "Default", lwd, "Default")
+        return [f.get_instance(g.functional_type(s["functional"]), lb)
+                for s, mol, basis, mg, lb in systems]
+
+    mixed = args.lwd.lower() == "gb300-mixed"
+    integs = make(args.lwd)
+    for integ in integs:  # the members share the GPU: 3 GB of work space each
+        integ.set_plan_params(scratch_gb=3.0)
+    Ps = [np.asfortranarray(s["P"]) for s, *_ in systems]
+    Vs = [np.zeros_like(P, order="F") for P in Ps]
+    tune = None
+    if mixed and not args.no_autotune:
+        t0 = time.perf_counter()
+        choice = {}
+        for integ, P in zip(integs, Ps):
+            ms, prm = integ.autotune(P)
+            key = (prm["pb_max_pts"], prm["nu2_weight"])
+            choice[key] = choice.get(key, 0) + 1
+        tune = dict(seconds=time.perf_counter() - t0,
+                    chosen={f"pts{k[0]}_w{int(k[1])}": v for k, v in sorted(choice.items())})
+    batch = g.IntegratorBatch(integs)
+    for _ in range(max(args.warmup, 2)):  # the first call captures the graph
+        batch.eval_exc_vxc(Ps, Vs)
+    sampler = ClockSampler(local)
+    barrier(dist)
+    sampler.start()
+    comp, wall = [], []
+    t_all0 = time.perf_counter()
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        exc = batch.eval_exc_vxc(Ps, Vs)
+        wall.append(time.perf_counter() - t0)
+        tm = batch.timings()
+        comp.append(tm["compute_ms"] * 1e-3)
+    t_all = time.perf_counter() - t_all0
+    barrier(dist)
+    clocks = sampler.stop()
+    value = reduce_max(dist, float(np.mean(comp)))
+    e2e = reduce_max(dist, float(np.mean(wall)))
+    if rank != 0:
+        return 0
+    stats = [i.plan_stats() for i in integs]
+    nbfs = [P.shape[0] for P in Ps]
+    launches = int(batch.timings()["gpu_launches"])
+    if mixed:
+        peaks = {}
+        pp = os.path.join(ROOT, "MEASURED_PEAKS.json")
+        if os.path.exists(pp):
+            peaks = json.load(open(pp))
+        peak = peaks.get("bf16_tflops_sustained")
+        src = "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)"
+        if peak is None:
+            peak, src = 1700.0, "fallback sustained bf16 1.7 PFLOP/s (of fallback)"
+        fl = sum(st["tensor_flops_x"] + st["tensor_flops_v"] for st in stats)
+        achieved = fl / value / 1e12
+        roofline = dict(bound="tensor", kernel="whole graph (all stages of all members)",
+                        achieved=achieved, peak=peak, unit="TFLOP/s", frac=achieved / peak,
+                        traffic=None, peak_source=src, algorithmic_flops_per_step=fl)
+    else:
+        fp64_peak = g.measure_fp64_peak()
+        fl = sum(4.0 * st["sum_npts_nbe2"] for st in stats)
+        achieved = fl / value / 1e12
+        roofline = dict(bound="fp64", kernel="whole graph (all stages of all members)",
+                        achieved=achieved, peak=fp64_peak, unit="TFLOP/s", frac=achieved / fp64_peak,
+                        traffic=None, peak_source="FP64 FMA probe measured in this run",
+                        algorithmic_flops_per_step=fl)
+    fp64_check = None
+    if mixed and not args.no_fp64_check:
+        batch = integs = None  # release the mixed plans first
+        i64 = make("GB300-FP64")
+        V64 = [np.zeros_like(P, order="F") for P in Ps]
+        b64 = g.IntegratorBatch(i64)
+        for _ in range(3):
+            e64 = b64.eval_exc_vxc(Ps, V64)
+        t64 = b64.timings()["compute_ms"] * 1e-3
+        fp64_check = dict(delta_exc=float(np.abs(exc - e64).max()),
+                          max_delta_vxc=float(max(np.abs(a - b).max() for a, b in zip(Vs, V64))),
+                          fp64_value=t64, speedup_vs_fp64=t64 / value,
+                          gates=dict(delta_exc=1e-8, max_delta_vxc=1e-8))
+    cpu = None
+    if not args.no_cpu_baseline:
+        # oracle on a sample of the largest member, scaled by sum npts*nbe^2
+        k = int(np.argmax([st["sum_npts_nbe2"] for st in stats]))
+        s, mol, basis, mg, lb = systems[k]
+        est, dt, ntask, share = time_cpu(W, basis, lb, s["P"], s["functional"],
+                                         budget_s=args.cpu_budget)
+        tot = sum(st["sum_npts_nbe2"] for st in stats)
+        scale = tot / stats[k]["sum_npts_nbe2"]
+        cpu = dict(value=est * scale, unit="s", cores=ncores, kind="port",
+                   sample=f"{ntask} tasks of the largest cluster ({share:.4f} of its sum "
+                          f"npts*nbe^2, {dt:.1f} s), scaled to all {len(systems)} clusters by "
+                          f"sum npts*nbe^2")
+    line = dict(
+        metric=METRIC, value=value, unit="s", n_gpus=args.gpus, steps=args.steps,
+        warmup=args.warmup, ms_per_step=value * 1e3, higher_is_better=False, scaling="weak",
+        vs_baseline=None,
+        dtype="bf16 digits (6 x 7 bit FP64 emulation, FP64 accumulate)" if mixed else "f64",
+        data="synthetic: seeded water clusters, even-tempered basis, P=CC^T (no dataset)",
+        config=dict(workload=WORKLOADS[args.config], config_index=args.config, lwd=args.lwd,
+                    members=len(systems), nbf_total=int(sum(nbfs)), nbf_max=int(max(nbfs)),
+                    npts=int(sum(st["npts"] for st in stats)),
+                    ntasks=int(sum(st["ntasks"] for st in stats)),
+                    l2="inputs larger than L2 (sum of members' P and VXC)",
+                    parallelism=f"replicas x{args.gpus}"),
+        e2e=dict(value=e2e, unit="s", h2d_bytes_per_step=int(sum(n * n * 8 for n in nbfs)),
+                 d2h_bytes_per_step=int(sum(n * n * 8 + 16 for n in nbfs)), pinned=True),
+        roofline=roofline, cpu_baseline=cpu, gpu_launches=launches,
+        graph_launches_per_step=1, clocks=clocks, fp64_check=fp64_check, autotune=tune,
+        exc_sum=float(np.sum(exc)),
+        setup_s=dict(load_balancer=t_lb, ssf_weights=t_w), timed_wall_s=t_all)
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 # ---------------------------------------------------------------------- main
 def main():
     ap = argparse.ArgumentParser()
@@ -214,6 +350,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-check", action="store_true",
                     help="mixed path: skip the FP64 device pass used for dEXC / dVXC")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="batched workload: keep the default plan parameters")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     dist = init_dist(ws)
@@ -225,7 +363,21 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return 0
-        s = W.config(args.config)["systems"][0]
+        systems = W.config(args.config)["systems"]
+        scale = 1.0
+        if len(systems) > 1:
+            # batched workload: the largest cluster is timed, the others are
+            # accounted for by sum npts*nbe^2 of their (host-built) task lists
+            costs = []
+            for sd in systems:
+                lbx = W.build_system(sd, device=False)[3]
+                costs.append(sum(lbx.task_info(i)["npts"] * lbx.task_info(i)["nbe"] ** 2
+                                 for i in range(lbx.ntasks())))
+            k = int(np.argmax(costs))
+            scale = sum(costs) / costs[k]
+            s = systems[k]
+        else:
+            s = systems[0]
         mol, basis, mg, lb = W.build_system(s, device=False)
         # the reference integrator needs weighted tasks: SSF by the CPU oracle
         import oracle
@@ -241,7 +393,7 @@ def main():
             est, dt, ntask, share = time_cpu(W, basis, lbw, s["P"], s["functional"],
                                              budget_s=args.cpu_budget / 2)
             if it >= args.warmup:
-                times.append(est)
+                times.append(est * scale)
         v = float(np.mean(times))
         line = dict(metric=METRIC, value=v, unit="s", n_gpus=args.gpus, steps=args.steps,
                     warmup=args.warmup, ms_per_step=v * 1e3, higher_is_better=False,
@@ -257,6 +409,9 @@ def main():
                     e2e=dict(value=v, unit="s", h2d_bytes_per_step=0, d2h_bytes_per_step=0))
         print(json.dumps(line), flush=True)
         return 0
+
+    if args.config == 3:
+        return run_batched(args, dist, rank, local, ncores)
 
     g.set_device(local)
     ctx = setup_workload(args.config, args.lwd)

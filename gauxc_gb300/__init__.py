@@ -17,15 +17,16 @@ import os
 
 import numpy as np
 
-from ._capi import (GauXCAtom, GauXCShell, GauXCStatus, MolecularWeightsSettingsC, check,
-                    load_library)
+from ._capi import (GauXCAtom, GauXCIntegrator, GauXCShell, GauXCStatus,
+                    MolecularWeightsSettingsC, check, load_library)
 
 __all__ = [
     "ExecutionSpace", "PruningScheme", "RadialQuad", "AtomicGridSizeDefault", "XCWeightAlg",
     "Molecule", "Shell", "BasisSet", "MolGrid", "MolGridFactory", "RuntimeEnvironment",
     "DeviceRuntimeEnvironment", "LoadBalancer", "LoadBalancerFactory",
     "MolecularWeightsSettings", "MolecularWeights", "MolecularWeightsFactory",
-    "functional_type", "XCIntegrator", "XCIntegratorFactory", "lib", "device_count",
+    "functional_type", "XCIntegrator", "XCIntegratorFactory", "IntegratorBatch", "lib",
+    "device_count",
     "ssf_weights", "collocation", "set_device", "measure_fp64_peak",
 ]
 
@@ -415,6 +416,62 @@ class XCIntegrator(_Handle):
                 "sum_pad_npts_nbe2", "scratch_bytes", "gpu_launches", "tensor_flops_x",
                 "tensor_flops_v"]
         return dict(zip(keys, list(out)))
+
+
+    def set_plan_params(self, pb_max_pts=256, nu2_weight=300.0, scratch_gb=0.0):
+        """Plan parameters (point-block size and merge weight of "GB300-Mixed",
+        work-space cap in GB, 0 = from free memory); the plan is rebuilt on the
+        next call."""
+        _call(_L.gauxc_gb300_integrator_set_plan_params, self._h, int(pb_max_pts),
+              float(nu2_weight), float(scratch_gb))
+
+    def autotune(self, P):
+        """Times the candidate plans on P, keeps the fastest.
+        Returns (compute_ms, dict(pb_max_pts=..., nu2_weight=...))."""
+        P = np.asfortranarray(P, dtype=np.float64)
+        pts, w = ctypes.c_int(), ctypes.c_double()
+        ms = _call(_L.gauxc_gb300_integrator_autotune, self._h, ctypes.c_int64(P.shape[0]),
+                   ctypes.c_int64(P.shape[1]), P.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                   ctypes.c_int64(P.shape[0]), ctypes.byref(pts), ctypes.byref(w))
+        return float(ms), dict(pb_max_pts=pts.value, nu2_weight=w.value)
+
+
+class IntegratorBatch(_Handle):
+    """Many integrators evaluated by one CUDA-graph launch per call.
+
+    The first call with a given set of arrays runs the members one by one and
+    captures the graph; later calls with the same arrays replay it.  The
+    arrays are page-locked in place while the batch uses them, so keep them
+    (and reuse them across SCF iterations)."""
+    _delete = "gauxc_gb300_batch_delete"
+
+    def __init__(self, integrators):
+        self.members = list(integrators)
+        arr = (GauXCIntegrator * len(self.members))(*[m._h for m in self.members])
+        super().__init__(_call(_L.gauxc_gb300_batch_new, arr, ctypes.c_int32(len(self.members))))
+
+    def eval_exc_vxc(self, Ps, VXCs):
+        """EXC of every member into a numpy array; VXC[i] written in place
+        (Fortran-ordered float64 arrays, nbf_i x nbf_i; None = EXC only)."""
+        n = len(self.members)
+        dp = ctypes.POINTER(ctypes.c_double)
+        for P in Ps:
+            if not (P.dtype == np.float64 and P.flags.f_contiguous):
+                raise ValueError("batch density matrices must be Fortran-ordered float64")
+        pp = (dp * n)(*[P.ctypes.data_as(dp) for P in Ps])
+        ldp = (ctypes.c_int64 * n)(*[P.shape[0] for P in Ps])
+        vv = (dp * n)(*[V.ctypes.data_as(dp) if V is not None else dp() for V in VXCs])
+        ldv = (ctypes.c_int64 * n)(*[V.shape[0] if V is not None else 0 for V in VXCs])
+        exc = np.zeros(n)
+        _call(_L.gauxc_gb300_batch_eval_exc_vxc_rks, self._h, pp, ldp, vv, ldv,
+              exc.ctypes.data_as(dp))
+        return exc
+
+    def timings(self):
+        out = (ctypes.c_double * 5)()
+        _call(_L.gauxc_gb300_batch_timings, self._h, out, 5)
+        return dict(zip(["compute_ms", "wall_ms", "graph_launch", "members", "gpu_launches"],
+                        list(out)))
 
 
 class XCIntegratorFactory:

@@ -31,6 +31,7 @@ GauXCMolecularWeights = _handle("GauXCMolecularWeights")
 GauXCMolecularWeightsFactory = _handle("GauXCMolecularWeightsFactory")
 GauXCFunctional = _handle("GauXCFunctional")
 GauXCIntegrator = _handle("GauXCIntegrator")
+GauXCGB300Batch = _handle("GauXCGB300Batch")
 
 
 class GauXCAtom(ctypes.Structure):
@@ -112,6 +113,14 @@ PROTOTYPES = {
     "gauxc_gb300_integrator_last_nel": (dbl, [S, GauXCIntegrator]),
     "gauxc_gb300_integrator_timings": (I, [S, GauXCIntegrator, P(dbl), I]),
     "gauxc_gb300_integrator_plan_stats": (I, [S, GauXCIntegrator, P(dbl), I]),
+    "gauxc_gb300_integrator_set_plan_params": (None, [S, GauXCIntegrator, I, dbl, dbl]),
+    "gauxc_gb300_integrator_autotune": (dbl, [S, GauXCIntegrator, i64, i64, P(dbl), i64, P(I),
+                                               P(dbl)]),
+    "gauxc_gb300_batch_new": (GauXCGB300Batch, [S, P(GauXCIntegrator), i32]),
+    "gauxc_gb300_batch_eval_exc_vxc_rks": (None, [S, GauXCGB300Batch, P(P(dbl)), P(i64),
+                                                  P(P(dbl)), P(i64), P(dbl)]),
+    "gauxc_gb300_batch_timings": (I, [S, GauXCGB300Batch, P(dbl), I]),
+    "gauxc_gb300_batch_delete": (None, [S, P(GauXCGB300Batch)]),
     "gauxc_gb300_integrator_set_profiling": (None, [S, GauXCIntegrator, b]),
     "gauxc_gb300_integrator_kernel_times": (I, [S, GauXCIntegrator, P(dbl), I]),
     "gauxc_gb300_measure_fp64_peak": (dbl, [S]),

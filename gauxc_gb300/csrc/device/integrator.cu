@@ -101,8 +101,8 @@ struct MBatch {
 class DeviceIntegrator {
  public:
   DeviceIntegrator(const LoadBalancer& lb, const XCFunctionalDesc& f, Precision prec,
-                   RuntimeEnv& rt)
-      : func_(f), prec_(prec), arena_(&rt), rt_(&rt) {
+                   RuntimeEnv& rt, const PlanParams& pp)
+      : func_(f), prec_(prec), params_(pp), arena_(&rt), rt_(&rt) {
     if (cuda_device_count() == 0) throw error("no CUDA device available for the device integrator");
     GB300_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     for (auto& e : ev_) GB300_CUDA(cudaEventCreate(&e));
@@ -124,6 +124,15 @@ class DeviceIntegrator {
 
   void eval(const double* P, int64_t ldp, double* VXC, int64_t ldvxc, double* EXC, double* NEL,
             bool den_only);
+  // All device work of one call on this integrator's stream, without waiting:
+  // P (host, ld ldp) in, VXC (host, ld ldvxc) out when do_vxc, {EXC, N_el}
+  // into en_host and the pipeline error flag into err_host.  Host buffers must
+  // be page-locked when the call is captured into a CUDA graph.  Returns the
+  // number of kernel launches.
+  int64_t enqueue(const double* P, int64_t ldp, double* VXC, int64_t ldvxc, double* en_host,
+                  int* err_host, bool do_vxc, bool events);
+  cudaStream_t stream() const { return stream_; }
+  int nbf() const { return nbf_; }
 
  private:
   void build(const LoadBalancer& lb);
@@ -132,6 +141,7 @@ class DeviceIntegrator {
 
   XCFunctionalDesc func_;
   Precision prec_;
+  PlanParams params_;
   Arena arena_;
   RuntimeEnv* rt_;
   cudaStream_t stream_ = nullptr;
@@ -293,6 +303,7 @@ void DeviceIntegrator::build(const LoadBalancer& lb) {
   else
     budget = rt_->fill_fraction * (double)free_b - static_bytes;
   if (const char* cap = std::getenv("GAUXC_GB300_SCRATCH_GB")) budget = std::min(budget, atof(cap) * 1e9);
+  if (params_.scratch_bytes > 0.) budget = std::min(budget, params_.scratch_bytes);
   budget = std::min(budget, 128e9);
   std::vector<int2> coll, dens;
   std::vector<int4> vx;
@@ -357,11 +368,11 @@ void DeviceIntegrator::build(const LoadBalancer& lb) {
 // Padded tensor-core work of one point block: density GEMM (M = basis rows
 // padded to kMTile, N = points padded to kNTile, K = basis padded to kBK)
 // plus the symmetric VXC GEMM (about half the M x N basis tiles, K = 2 points).
-static double pb_cost(int npts, int nu) {
+static double pb_cost(int npts, int nu, double nu2_weight) {
   const double np = (double)round_up(npts, kNTile);
   const double m = (double)round_up(nu, kMTile), n = (double)round_up(nu, kNTile),
                k = (double)round_up(nu, kBK);
-  return m * np * k + m * n * np;
+  return m * np * k + m * n * np + nu2_weight * m * n;
 }
 
 // Point blocks for the tensor-core path: consecutive tasks of one parent atom
@@ -387,20 +398,23 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
     for (int x : sl) n += bs.shells[x].size();
     return n;
   };
+  const int maxp = std::max(kNTile, std::min(kPBMaxPts, params_.pb_max_pts / kNTile * kNTile));
+  const double w2 = std::max(0., params_.nu2_weight);
   std::vector<PB> pbs;
   for (int t = 0; t < (int)tasks.size(); ++t) {
     const XCTask& tt = tasks[t];
-    for (int p0 = 0; p0 < tt.npts; p0 += kPBMaxPts) {
-      const int p1 = std::min(tt.npts, p0 + kPBMaxPts);
+    for (int p0 = 0; p0 < tt.npts; p0 += maxp) {
+      const int p1 = std::min(tt.npts, p0 + maxp);
       bool merged = false;
       if (!pbs.empty() && pbs.back().iparent == tt.iParent &&
-          pbs.back().npts + (p1 - p0) <= kPBMaxPts) {
+          pbs.back().npts + (p1 - p0) <= maxp) {
         PB& b = pbs.back();
         std::vector<int> u;
         std::set_union(b.shells.begin(), b.shells.end(), tt.shell_list.begin(),
                        tt.shell_list.end(), std::back_inserter(u));
         const int nu = nbe_of(u);
-        if (pb_cost(b.npts + (p1 - p0), nu) <= pb_cost(b.npts, b.nu) + pb_cost(p1 - p0, tt.nbe)) {
+        if (pb_cost(b.npts + (p1 - p0), nu, w2) <=
+            pb_cost(b.npts, b.nu, w2) + pb_cost(p1 - p0, tt.nbe, w2)) {
           b.shells.swap(u);
           b.nu = nu;
           b.npts += p1 - p0;
@@ -496,6 +510,7 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
   double budget = rt_->user_mem ? (double)rt_->user_bytes - rt_->user_used - static_bytes
                                 : rt_->fill_fraction * (double)free_b - static_bytes;
   if (const char* cap = std::getenv("GAUXC_GB300_SCRATCH_GB")) budget = std::min(budget, atof(cap) * 1e9);
+  if (params_.scratch_bytes > 0.) budget = std::min(budget, params_.scratch_bytes);
   budget = std::min(budget, 96e9);
   std::vector<int2> coll;
   std::vector<OzItem> xi, vi;
@@ -638,16 +653,14 @@ int64_t DeviceIntegrator::eval_mixed_batches(bool do_vxc) {
   return launches;
 }
 
-void DeviceIntegrator::eval(const double* P, int64_t ldp, double* VXC, int64_t ldvxc, double* EXC,
-                            double* NEL, bool den_only) {
+int64_t DeviceIntegrator::enqueue(const double* P, int64_t ldp, double* VXC, int64_t ldvxc,
+                                  double* en_host, int* err_host, bool do_vxc, bool events) {
   cudaStream_t s = stream_;
   const size_t row = (size_t)nbf_ * sizeof(double);
-  auto t_host0 = std::chrono::steady_clock::now();
-  GB300_CUDA(cudaEventRecord(ev_[0], s));
+  if (events) GB300_CUDA(cudaEventRecord(ev_[0], s));
   GB300_CUDA(cudaMemcpy2DAsync(P_, row, P, (size_t)ldp * sizeof(double), row, nbf_,
                                cudaMemcpyHostToDevice, s));
-  GB300_CUDA(cudaEventRecord(ev_[1], s));
-  const bool do_vxc = (VXC != nullptr) && !den_only;
+  if (events) GB300_CUDA(cudaEventRecord(ev_[1], s));
   if (do_vxc) GB300_CUDA(cudaMemsetAsync(A_, 0, (size_t)nbf_ * nbf_ * sizeof(double), s));
   int64_t launches = 0;
   pev_used_ = 0;
@@ -685,16 +698,25 @@ void DeviceIntegrator::eval(const double* P, int64_t ldp, double* VXC, int64_t l
     launch_reduce_partials(partials_, ndens_, out_, s);
     return (int64_t)1;
   });
-  GB300_CUDA(cudaEventRecord(ev_[2], s));
+  if (events) GB300_CUDA(cudaEventRecord(ev_[2], s));
   if (do_vxc)
     GB300_CUDA(cudaMemcpy2DAsync(VXC, (size_t)ldvxc * sizeof(double), V_, row, row, nbf_,
                                  cudaMemcpyDeviceToHost, s));
-  double en[2];
-  GB300_CUDA(cudaMemcpyAsync(en, out_, sizeof(en), cudaMemcpyDeviceToHost, s));
+  GB300_CUDA(cudaMemcpyAsync(en_host, out_, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GB300_CUDA(cudaMemcpyAsync(err_host, err_, sizeof(int), cudaMemcpyDeviceToHost, s));
+  if (events) GB300_CUDA(cudaEventRecord(ev_[3], s));
+  stats.gpu_launches = launches;
+  return launches;
+}
+
+void DeviceIntegrator::eval(const double* P, int64_t ldp, double* VXC, int64_t ldvxc, double* EXC,
+                            double* NEL, bool den_only) {
+  auto t_host0 = std::chrono::steady_clock::now();
+  const bool do_vxc = (VXC != nullptr) && !den_only;
+  double en[2] = {0., 0.};
   int herr = 0;
-  GB300_CUDA(cudaMemcpyAsync(&herr, err_, sizeof(int), cudaMemcpyDeviceToHost, s));
-  GB300_CUDA(cudaEventRecord(ev_[3], s));
-  GB300_CUDA(cudaStreamSynchronize(s));
+  const int64_t launches = enqueue(P, ldp, VXC, ldvxc, en, &herr, do_vxc, true);
+  GB300_CUDA(cudaStreamSynchronize(stream_));
   if (herr)
     throw error("a tensor-core pipeline wait expired on the device (error code " +
                 std::to_string(herr) + ")");
@@ -709,7 +731,6 @@ void DeviceIntegrator::eval(const double* P, int64_t ldp, double* VXC, int64_t l
   timings["compute_ms"] = comp;
   timings["d2h_ms"] = d2h;
   timings["wall_ms"] = std::chrono::duration<double, std::milli>(t_host1 - t_host0).count();
-  stats.gpu_launches = launches;
   timings["gpu_launches"] = (double)launches;
   for (int k = 0; k < 5; ++k) {
     kclass_ms[k] = 0.;
@@ -732,7 +753,7 @@ void ensure_plan(XCIntegratorHandle& h) {
   if (!h.dev || h.dev->generation != h.lb->generation) {
     h.dev.reset();
     if (h.rt && h.rt->user_mem) h.rt->user_used = 0;
-    h.dev = std::make_shared<DeviceIntegrator>(*h.lb, *h.func, h.prec, *h.rt);
+    h.dev = std::make_shared<DeviceIntegrator>(*h.lb, *h.func, h.prec, *h.rt, h.params);
   }
   h.dev->profiling = h.profiling;
 }
@@ -792,5 +813,271 @@ PlanStats integrator_plan_stats(XCIntegratorHandle& h) {
   ensure_plan(h);
   return h.dev->stats;
 }
+
+void integrator_set_plan_params(XCIntegratorHandle& h, const PlanParams& p) {
+  if (!(p.scratch_bytes >= 0.)) throw error("scratch cap must be non-negative");
+  if (p.pb_max_pts < kNTile || p.pb_max_pts > kPBMaxPts)
+    throw error("point-block size must lie in [" + std::to_string(kNTile) + ", " +
+                std::to_string(kPBMaxPts) + "]");
+  if (!(p.nu2_weight >= 0.)) throw error("merge weight must be non-negative");
+  h.params = p;
+  h.dev.reset();  // rebuilt with the new parameters on the next call
+}
+
+// Candidate plans: point-block sizes x weights of the per-block gather and
+// scatter work (union basis squared) in the merge rule.  Each candidate is
+// built and timed on one warm call; the fastest stays in place.
+double integrator_autotune(XCIntegratorHandle& h, const double* P, int64_t ldp, PlanParams* best) {
+  if (!P) throw error("null density matrix");
+  const int64_t nbf = h.lb->basis->nbf;
+  check_dims(h, nbf, nbf, ldp);
+  std::vector<double> V((size_t)nbf * nbf);
+  std::vector<PlanParams> cands;
+  if (h.prec == Precision::Mixed) {
+    for (int pts : {128, 192, 256})
+      for (double w : {0., 300.}) cands.push_back(PlanParams{pts, w, h.params.scratch_bytes});
+  } else {
+    cands.push_back(h.params);
+  }
+  double best_ms = -1.;
+  PlanParams bp = h.params;
+  for (const PlanParams& c : cands) {
+    h.params = c;
+    h.dev.reset();
+    ensure_plan(h);
+    double exc = 0., nel = 0.;
+    h.dev->eval(P, ldp, V.data(), nbf, &exc, &nel, false);
+    h.dev->eval(P, ldp, V.data(), nbf, &exc, &nel, false);
+    const double ms = h.dev->timings["compute_ms"];
+    if (best_ms < 0. || ms < best_ms) {
+      best_ms = ms;
+      bp = c;
+    }
+  }
+  if (h.params.pb_max_pts != bp.pb_max_pts || h.params.nu2_weight != bp.nu2_weight ||
+      h.params.scratch_bytes != bp.scratch_bytes) {
+    h.params = bp;
+    h.dev.reset();
+    ensure_plan(h);
+  }
+  if (best) *best = bp;
+  return best_ms;
+}
+
+// ---------------------------------------------------------------- batches
+// One CUDA graph per set of caller buffers: the root stream forks into every
+// member integrator's stream, each member enqueues its whole call (P in,
+// kernels, VXC / EXC / error flag out) and the root joins them.  Replaying
+// the graph is then a single launch per SCF iteration, and the members'
+// branches run concurrently on the GPU.
+class IntegratorBatch {
+ public:
+  explicit IntegratorBatch(const std::vector<XCIntegratorHandle*>& hs) : hs_(hs) {
+    if (hs_.empty()) throw error("empty integrator batch");
+    for (auto* h : hs_)
+      if (!h) throw error("null integrator in batch");
+    // Members share the device: each one without its own work-space cap gets
+    // an equal share of the memory free now (plus what its current plan holds).
+    size_t free_b = 0, total_b = 0;
+    GB300_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    int uncapped = 0;
+    for (auto* h : hs_)
+      if (h->params.scratch_bytes <= 0.) ++uncapped;
+    if (uncapped) {
+      double held = 0.;
+      for (auto* h : hs_)
+        if (h->params.scratch_bytes <= 0. && h->dev) held += h->dev->stats.scratch_bytes;
+      const double share = 0.8 * ((double)free_b + held) / uncapped;
+      for (auto* h : hs_)
+        if (h->params.scratch_bytes <= 0.) {
+          h->params.scratch_bytes = std::max(share, 256e6);
+          h->dev.reset();
+        }
+    }
+    GB300_CUDA(cudaStreamCreateWithFlags(&root_, cudaStreamNonBlocking));
+    GB300_CUDA(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));
+    GB300_CUDA(cudaEventCreate(&t0_));
+    GB300_CUDA(cudaEventCreate(&t1_));
+    joins_.resize(hs_.size());
+    for (auto& e : joins_) GB300_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    GB300_CUDA(cudaMallocHost(&en_, 2 * hs_.size() * sizeof(double)));
+    GB300_CUDA(cudaMallocHost(&err_, hs_.size() * sizeof(int)));
+  }
+  ~IntegratorBatch() {
+    release_graph();
+    unregister_all();
+    for (auto& e : joins_) cudaEventDestroy(e);
+    cudaEventDestroy(fork_);
+    cudaEventDestroy(t0_);
+    cudaEventDestroy(t1_);
+    cudaStreamDestroy(root_);
+    cudaFreeHost(en_);
+    cudaFreeHost(err_);
+  }
+
+  void eval(const double* const* P, const int64_t* ldp, double* const* VXC, const int64_t* ldvxc,
+            double* EXC) {
+    const size_t n = hs_.size();
+    auto t_host0 = std::chrono::steady_clock::now();
+    bool same = exec_ != nullptr && cap_dev_.size() == n;
+    for (size_t i = 0; i < n; ++i) {
+      XCIntegratorHandle& h = *hs_[i];
+      if (!P[i]) throw error("null density matrix in batch member " + std::to_string(i));
+      const int64_t nbf = h.lb->basis->nbf;
+      check_dims(h, nbf, nbf, ldp[i]);
+      if (VXC[i] && ldvxc[i] < nbf) throw error("Invalid LDVXC");
+      ensure_plan(h);
+      if (same && (cap_dev_[i] != h.dev.get() || cap_P_[i] != P[i] || cap_V_[i] != VXC[i] ||
+                   cap_ldp_[i] != ldp[i] || cap_ldv_[i] != (VXC[i] ? ldvxc[i] : 0)))
+        same = false;
+    }
+    if (!same) {
+      // First call with these buffers: plain calls (which also set up every
+      // kernel), then capture the graph for the next calls.
+      for (size_t i = 0; i < n; ++i) {
+        XCIntegratorHandle& h = *hs_[i];
+        double nel = 0.;
+        h.dev->eval(P[i], ldp[i], VXC[i], VXC[i] ? ldvxc[i] : 0, &EXC[i], &nel, false);
+        h.last_exc = EXC[i];
+        h.last_nel = nel;
+      }
+      capture(P, ldp, VXC, ldvxc);
+      timings_["graph_launch"] = 0.;
+      timings_["wall_ms"] =
+          std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_host0).count();
+      return;
+    }
+    GB300_CUDA(cudaEventRecord(t0_, root_));
+    GB300_CUDA(cudaGraphLaunch(exec_, root_));
+    GB300_CUDA(cudaEventRecord(t1_, root_));
+    GB300_CUDA(cudaStreamSynchronize(root_));
+    for (size_t i = 0; i < n; ++i) {
+      if (err_[i])
+        throw error("a tensor-core pipeline wait expired on the device (batch member " +
+                    std::to_string(i) + ", error code " + std::to_string(err_[i]) + ")");
+      EXC[i] = en_[2 * i];
+      hs_[i]->last_exc = en_[2 * i];
+      hs_[i]->last_nel = en_[2 * i + 1];
+    }
+    float ms = 0.f;
+    GB300_CUDA(cudaEventElapsedTime(&ms, t0_, t1_));
+    timings_["graph_launch"] = 1.;
+    timings_["compute_ms"] = ms;  // whole graph: H2D, kernels, D2H of every member
+    timings_["wall_ms"] =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_host0).count();
+    timings_["members"] = (double)n;
+    timings_["gpu_launches"] = (double)launches_;
+  }
+
+  const std::map<std::string, double>& timings() const { return timings_; }
+
+ private:
+  void release_graph() {
+    if (exec_) cudaGraphExecDestroy(exec_);
+    if (graph_) cudaGraphDestroy(graph_);
+    exec_ = nullptr;
+    graph_ = nullptr;
+  }
+  void unregister_all() {
+    for (void* p : registered_) cudaHostUnregister(p);
+    registered_.clear();
+  }
+  // Page-locks [p, p + bytes) in place unless it already is.
+  void pin(const void* p, size_t bytes) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) == cudaSuccess &&
+        (a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeDevice ||
+         a.type == cudaMemoryTypeManaged))
+      return;
+    cudaGetLastError();
+    const cudaError_t e = cudaHostRegister(const_cast<void*>(p), bytes, cudaHostRegisterDefault);
+    if (e == cudaErrorHostMemoryAlreadyRegistered) {
+      cudaGetLastError();
+      return;
+    }
+    GB300_CUDA(e);
+    registered_.push_back(const_cast<void*>(p));
+  }
+  void capture(const double* const* P, const int64_t* ldp, double* const* VXC,
+               const int64_t* ldvxc) {
+    const size_t n = hs_.size();
+    release_graph();
+    unregister_all();
+    cap_dev_.assign(n, nullptr);
+    cap_P_.assign(n, nullptr);
+    cap_V_.assign(n, nullptr);
+    cap_ldp_.assign(n, 0);
+    cap_ldv_.assign(n, 0);
+    for (size_t i = 0; i < n; ++i) {
+      const int64_t nbf = hs_[i]->lb->basis->nbf;
+      pin(P[i], (size_t)((nbf - 1) * ldp[i] + nbf) * sizeof(double));
+      if (VXC[i]) pin(VXC[i], (size_t)((nbf - 1) * ldvxc[i] + nbf) * sizeof(double));
+    }
+    std::vector<bool> prof(n);
+    for (size_t i = 0; i < n; ++i) {
+      prof[i] = hs_[i]->dev->profiling;
+      hs_[i]->dev->profiling = false;  // no event records inside the graph
+    }
+    launches_ = 0;
+    GB300_CUDA(cudaStreamBeginCapture(root_, cudaStreamCaptureModeThreadLocal));
+    bool ok = false;
+    try {
+      GB300_CUDA(cudaEventRecord(fork_, root_));
+      for (size_t i = 0; i < n; ++i) {
+        DeviceIntegrator& d = *hs_[i]->dev;
+        GB300_CUDA(cudaStreamWaitEvent(d.stream(), fork_, 0));
+        launches_ += d.enqueue(P[i], ldp[i], VXC[i], VXC[i] ? ldvxc[i] : 0, en_ + 2 * i, err_ + i,
+                               VXC[i] != nullptr, false);
+        GB300_CUDA(cudaEventRecord(joins_[i], d.stream()));
+        GB300_CUDA(cudaStreamWaitEvent(root_, joins_[i], 0));
+      }
+      ok = true;
+    } catch (...) {
+      cudaGraph_t g = nullptr;
+      cudaStreamEndCapture(root_, &g);
+      if (g) cudaGraphDestroy(g);
+      for (size_t i = 0; i < n; ++i) hs_[i]->dev->profiling = prof[i];
+      throw;
+    }
+    GB300_CUDA(cudaStreamEndCapture(root_, &graph_));
+    for (size_t i = 0; i < n; ++i) hs_[i]->dev->profiling = prof[i];
+    if (!ok || !graph_) throw error("graph capture failed");
+    GB300_CUDA(cudaGraphInstantiate(&exec_, graph_, 0));
+    for (size_t i = 0; i < n; ++i) {
+      cap_dev_[i] = hs_[i]->dev.get();
+      cap_P_[i] = P[i];
+      cap_V_[i] = VXC[i];
+      cap_ldp_[i] = ldp[i];
+      cap_ldv_[i] = VXC[i] ? ldvxc[i] : 0;
+    }
+  }
+
+  std::vector<XCIntegratorHandle*> hs_;
+  cudaStream_t root_ = nullptr;
+  cudaEvent_t fork_ = nullptr, t0_ = nullptr, t1_ = nullptr;
+  std::vector<cudaEvent_t> joins_;
+  cudaGraph_t graph_ = nullptr;
+  cudaGraphExec_t exec_ = nullptr;
+  double* en_ = nullptr;
+  int* err_ = nullptr;
+  int64_t launches_ = 0;
+  std::vector<DeviceIntegrator*> cap_dev_;
+  std::vector<const double*> cap_P_;
+  std::vector<double*> cap_V_;
+  std::vector<int64_t> cap_ldp_, cap_ldv_;
+  std::vector<void*> registered_;
+  std::map<std::string, double> timings_;
+};
+
+std::shared_ptr<IntegratorBatch> batch_new(const std::vector<XCIntegratorHandle*>& hs) {
+  return std::make_shared<IntegratorBatch>(hs);
+}
+
+void batch_eval_exc_vxc(IntegratorBatch& b, const double* const* P, const int64_t* ldp,
+                        double* const* VXC, const int64_t* ldvxc, double* EXC) {
+  b.eval(P, ldp, VXC, ldvxc, EXC);
+}
+
+std::map<std::string, double> batch_timings(const IntegratorBatch& b) { return b.timings(); }
 
 }  // namespace gb300

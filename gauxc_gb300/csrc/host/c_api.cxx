@@ -77,6 +77,11 @@ struct LBFactory {
   bool device;
   std::string kernel;
 };
+// A batch keeps its member integrators alive.
+struct BatchHandle {
+  std::vector<std::shared_ptr<XCIntegratorHandle>> members;
+  std::shared_ptr<IntegratorBatch> batch;
+};
 struct MWFactory {
   bool device;
   GauXCMolecularWeightsSettings settings;
@@ -127,6 +132,7 @@ void gauxc_object_delete(GauXCStatus* status, void** handle) {
       break;
     case GauXC_Type_Functional: gauxc_functional_delete(status, (GauXCFunctional*)*handle); break;
     case GauXC_Type_Integrator: gauxc_integrator_delete(status, (GauXCIntegrator*)*handle); break;
+    case GauXC_Type_GB300Batch: gauxc_gb300_batch_delete(status, (GauXCGB300Batch*)*handle); break;
     default: status_fail(status, "unknown handle type");
   }
 }
@@ -715,6 +721,98 @@ int gauxc_gb300_integrator_kernel_times(GauXCStatus* status, const GauXCIntegrat
   int n = 0;
   for (; n < (int)v.size() && n < nmax; ++n) out[n] = v[n];
   return n;
+}
+
+void gauxc_gb300_integrator_set_plan_params(GauXCStatus* status, const GauXCIntegrator integrator,
+                                            int pb_max_pts, double nu2_weight,
+                                            double scratch_gb) {
+  status_init(status);
+  if (!check(status, integrator, GauXC_Type_Integrator, "Integrator")) return;
+  guarded(status, [&] {
+    integrator_set_plan_params(*deref<XCIntegratorHandle>(integrator.ptr),
+                               PlanParams{pb_max_pts, nu2_weight, scratch_gb * 1e9});
+  });
+}
+
+double gauxc_gb300_integrator_autotune(GauXCStatus* status, const GauXCIntegrator integrator,
+                                       int64_t m, int64_t n, const double* P, int64_t ldp,
+                                       int* pb_max_pts, double* nu2_weight) {
+  status_init(status);
+  if (!check(status, integrator, GauXC_Type_Integrator, "Integrator")) return 0.;
+  if (!P) {
+    status_fail(status, "Density matrix pointer cannot be null");
+    return 0.;
+  }
+  double ms = 0.;
+  guarded(status, [&] {
+    XCIntegratorHandle& h = *deref<XCIntegratorHandle>(integrator.ptr);
+    if (m != n || m != h.lb->basis->nbf) throw error("P Must Have Same Dimension as Basis");
+    PlanParams best;
+    ms = integrator_autotune(h, P, ldp, &best);
+    if (pb_max_pts) *pb_max_pts = best.pb_max_pts;
+    if (nu2_weight) *nu2_weight = best.nu2_weight;
+  });
+  return ms;
+}
+
+GauXCGB300Batch gauxc_gb300_batch_new(GauXCStatus* status, const GauXCIntegrator* integrators,
+                                      int32_t n) {
+  status_init(status);
+  GauXCGB300Batch b{};
+  if (!integrators || n <= 0) {
+    status_fail(status, "Batch needs at least one integrator");
+    return b;
+  }
+  for (int32_t i = 0; i < n; ++i)
+    if (!check(status, integrators[i], GauXC_Type_Integrator, "Integrator")) return b;
+  guarded(status, [&] {
+    auto bh = std::make_shared<BatchHandle>();
+    std::vector<XCIntegratorHandle*> raw;
+    for (int32_t i = 0; i < n; ++i) {
+      bh->members.push_back(deref<XCIntegratorHandle>(integrators[i].ptr));
+      raw.push_back(bh->members.back().get());
+    }
+    bh->batch = batch_new(raw);
+    b = make_handle<GauXCGB300Batch>(GauXC_Type_GB300Batch, bh);
+  });
+  return b;
+}
+
+void gauxc_gb300_batch_eval_exc_vxc_rks(GauXCStatus* status, const GauXCGB300Batch batch,
+                                        const double* const* P, const int64_t* ldp,
+                                        double* const* VXC, const int64_t* ldvxc, double* EXC) {
+  status_init(status);
+  if (!check(status, batch, GauXC_Type_GB300Batch, "Batch")) return;
+  if (!P || !ldp || !EXC) return status_fail(status, "P, ldp and EXC arrays cannot be null");
+  guarded(status, [&] {
+    auto& bh = *deref<BatchHandle>(batch.ptr);
+    const size_t n = bh.members.size();
+    std::vector<double*> V(n, nullptr);
+    std::vector<int64_t> lv(n, 0);
+    if (VXC)
+      for (size_t i = 0; i < n; ++i) {
+        V[i] = VXC[i];
+        lv[i] = ldvxc ? ldvxc[i] : 0;
+      }
+    batch_eval_exc_vxc(*bh.batch, P, ldp, V.data(), lv.data(), EXC);
+  });
+}
+
+int gauxc_gb300_batch_timings(GauXCStatus* status, const GauXCGB300Batch batch, double* out,
+                              int nmax) {
+  status_init(status);
+  if (!check(status, batch, GauXC_Type_GB300Batch, "Batch")) return 0;
+  auto t = batch_timings(*deref<BatchHandle>(batch.ptr)->batch);
+  const double v[5] = {t["compute_ms"], t["wall_ms"], t["graph_launch"], t["members"],
+                       t["gpu_launches"]};
+  int k = 0;
+  for (; k < 5 && k < nmax; ++k) out[k] = v[k];
+  return k;
+}
+
+void gauxc_gb300_batch_delete(GauXCStatus* status, GauXCGB300Batch* batch) {
+  status_init(status);
+  destroy<BatchHandle>(batch);
 }
 
 double gauxc_gb300_measure_fp64_peak(GauXCStatus* status) {

@@ -32,6 +32,15 @@ struct PlanStats {
   double tensor_flops_x = 0., tensor_flops_v = 0.;  // BF16 MMA flops per call (mixed path)
 };
 
+// Tunable parameters of the tensor-core plan (point blocks).
+struct PlanParams {
+  int pb_max_pts = 256;       // points per point block (multiple of 64, <= 256)
+  double nu2_weight = 300.;   // merge-rule cost of one union-basis element squared
+                              // (gather / scatter work per block), in tile MACs
+  double scratch_bytes = 0.;  // cap of the per-pass work space (0 = from free memory);
+                              // a plan that needs more runs in several passes
+};
+
 class DeviceIntegrator;
 
 struct XCIntegratorHandle {
@@ -42,6 +51,7 @@ struct XCIntegratorHandle {
   std::shared_ptr<DeviceIntegrator> dev;
   double last_exc = 0., last_nel = 0.;
   bool profiling = false;
+  PlanParams params;
 };
 
 // eval_exc_vxc for RKS; VXC may be null (EXC only).  Throws gb300::error.
@@ -55,6 +65,22 @@ PlanStats integrator_plan_stats(XCIntegratorHandle& h);
 // zmat, vxc, other): {ms, launches} pairs of the last call.
 void integrator_set_profiling(XCIntegratorHandle& h, bool on);
 std::vector<double> integrator_kernel_times(const XCIntegratorHandle& h);
+// Sets the tensor-core plan parameters; the plan is rebuilt on the next call.
+void integrator_set_plan_params(XCIntegratorHandle& h, const PlanParams& p);
+// Times one call for each candidate plan (point-block sizes x merge weights)
+// on density P and keeps the fastest; returns its compute time in ms and
+// writes the chosen parameters to *best.
+double integrator_autotune(XCIntegratorHandle& h, const double* P, int64_t ldp, PlanParams* best);
+
+// Many integrators evaluated by one CUDA-graph launch per call.
+class IntegratorBatch;
+std::shared_ptr<IntegratorBatch> batch_new(const std::vector<XCIntegratorHandle*>& hs);
+// EXC[i] for every member; VXC[i] may be null (EXC only).  Host buffers are
+// page-locked in place (cudaHostRegister) and stay registered until the
+// batch is destroyed or other buffers are passed.
+void batch_eval_exc_vxc(IntegratorBatch& b, const double* const* P, const int64_t* ldp,
+                        double* const* VXC, const int64_t* ldvxc, double* EXC);
+std::map<std::string, double> batch_timings(const IntegratorBatch& b);
 
 // FP64 FMA throughput probe (TFLOP/s) on the current device.
 double measure_fp64_peak();

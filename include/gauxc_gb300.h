@@ -50,7 +50,9 @@ enum GauXC_Type {
   GauXC_Type_MolecularWeights = 7,
   GauXC_Type_MolecularWeightsFactory = 8,
   GauXC_Type_Functional = 9,
-  GauXC_Type_Integrator = 10
+  GauXC_Type_Integrator = 10,
+  /* extension: handle of a batch of integrators (gauxc_gb300_batch_new) */
+  GauXC_Type_GB300Batch = 64
 };
 
 /* include/gauxc/c/types.h:42 */
@@ -125,6 +127,8 @@ typedef struct GauXCMolecularWeights { GauXCHeader hdr; void* ptr; } GauXCMolecu
 typedef struct GauXCMolecularWeightsFactory { GauXCHeader hdr; void* ptr; } GauXCMolecularWeightsFactory;
 typedef struct GauXCFunctional { GauXCHeader hdr; void* ptr; } GauXCFunctional;
 typedef struct GauXCIntegrator { GauXCHeader hdr; void* ptr; } GauXCIntegrator;
+/* extension: many integrators evaluated by one CUDA-graph launch */
+typedef struct GauXCGB300Batch { GauXCHeader hdr; void* ptr; } GauXCGB300Batch;
 
 /* include/gauxc/c/molecular_weights.h:34 */
 typedef struct GauXCMolecularWeightsSettings {
@@ -301,6 +305,46 @@ void gauxc_gb300_ssf_weights_noalloc(GauXCStatus* status, int64_t npts, int32_t 
 void gauxc_gb300_collocation(GauXCStatus* status, const GauXCBasisSet basis, int64_t npts,
                              const double* points, int32_t nshells, const int32_t* shell_list,
                              double* phi, double* dphi_x, double* dphi_y, double* dphi_z);
+
+/* ---- batched evaluation and plan tuning (no counterpart in the reference;
+   the per-member work is gauxc_integrator_eval_exc_vxc_rks, xc_integrator.h:180) */
+
+/* Plan parameters: points per point block of a "GB300-Mixed" integrator
+   (multiple of 64, 64..256), the weight of a block's union-basis gather and
+   scatter work in the block-merge rule, and a cap (GB, 0 = from free memory)
+   on the device work space of one pass over the grid; a plan needing more
+   runs in several passes.  The plan is rebuilt on the next call. */
+void gauxc_gb300_integrator_set_plan_params(GauXCStatus* status, const GauXCIntegrator integrator,
+                                            int pb_max_pts, double nu2_weight, double scratch_gb);
+/* Autotuner: builds and times one call per candidate plan (point-block sizes
+   128/192/256 x merge weights 0/300 for "GB300-Mixed"; the current plan
+   otherwise) on density P and keeps the fastest.  Returns its compute time in
+   ms and the chosen parameters. */
+double gauxc_gb300_integrator_autotune(GauXCStatus* status, const GauXCIntegrator integrator,
+                                       int64_t m, int64_t n, const double* P, int64_t ldp,
+                                       int* pb_max_pts, double* nu2_weight);
+/* A batch over n integrators (any mix of molecules, functionals and
+   precisions).  gauxc_gb300_batch_eval_exc_vxc_rks evaluates every member:
+   P[i] (nbf_i x nbf_i, ld ldp[i]) in, EXC[i] and VXC[i] (ld ldvxc[i]; NULL =
+   EXC only) out.  The first call with a given set of buffers runs the members
+   one by one and captures a CUDA graph of all of them (H2D, kernels, D2H on
+   one stream per member, forked from and joined into one root stream); later
+   calls with the same buffers are a single graph launch.  Members without a
+   work-space cap (gauxc_gb300_integrator_set_plan_params) get an equal share
+   of the device memory free when the batch is created.  The buffers are
+   page-locked in place (cudaHostRegister) until the batch is deleted or other
+   buffers are passed; they must stay valid meanwhile.  Members must not be
+   evaluated concurrently from other threads. */
+GauXCGB300Batch gauxc_gb300_batch_new(GauXCStatus* status, const GauXCIntegrator* integrators,
+                                      int32_t n);
+void gauxc_gb300_batch_eval_exc_vxc_rks(GauXCStatus* status, const GauXCGB300Batch batch,
+                                        const double* const* P, const int64_t* ldp,
+                                        double* const* VXC, const int64_t* ldvxc, double* EXC);
+/* {compute_ms (graph, CUDA events), wall_ms, graph_launch (0/1), members,
+   gpu_launches} of the last call; returns the count written. */
+int gauxc_gb300_batch_timings(GauXCStatus* status, const GauXCGB300Batch batch, double* out,
+                              int nmax);
+void gauxc_gb300_batch_delete(GauXCStatus* status, GauXCGB300Batch* batch);
 
 #ifdef __cplusplus
 }
