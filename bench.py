@@ -3,6 +3,11 @@
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
                   [--config IDX] [--lwd Default|GB300-FP64|GB300-Mixed]
 
+Default: workload 4 (256 waters, PBE, 15360 bf) on the tensor-core path
+("GB300-Mixed"), with the plain FP64 device path run once beside it for the
+speed-up and the |dEXC| / max|dVXC| check.  Workload 3 is the batched case
+(64 clusters, every SCF iteration one CUDA-graph launch).
+
 A step is one eval_exc_vxc(P) call of the workload: the device-resident plan
 (tasks, SSF weights, maps) is built during the untimed warm-up; each timed
 call copies P in, runs the whole XC pass and copies VXC out.
@@ -344,8 +349,10 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", type=int, default=1)
-    ap.add_argument("--lwd", default="Default")
+    # default: the headline workload (256 waters, PBE) on the tensor-core path,
+    # with the FP64 device path timed beside it for the speed-up and the errors
+    ap.add_argument("--config", type=int, default=4)
+    ap.add_argument("--lwd", default="GB300-Mixed")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-check", action="store_true",
@@ -379,15 +386,9 @@ def main():
         else:
             s = systems[0]
         mol, basis, mg, lb = W.build_system(s, device=False)
-        # the reference integrator needs weighted tasks: SSF by the CPU oracle
-        import oracle
-        tasks = lb.get_tasks()
-        pts = np.concatenate([t["points"] for t in tasks])
-        wts = np.concatenate([t["weights"] for t in tasks])
-        ip = np.concatenate([np.full(t["npts"], t["iParent"], np.int32) for t in tasks])
-        dn = np.concatenate([np.full(t["npts"], t["dist_nearest"]) for t in tasks])
-        wm = oracle.ssf_weights(pts, ip, dn, mol.coords(), wts)
-        lbw = _WeightedTasks(tasks, wm)
+        # the reference integrator needs weighted tasks: SSF by the CPU oracle,
+        # for the points of the sampled tasks only
+        lbw = _SampledWeightedTasks(lb, mol)
         times = []
         for it in range(args.warmup + args.steps):
             est, dt, ntask, share = time_cpu(W, basis, lbw, s["P"], s["functional"],
@@ -537,6 +538,31 @@ def main():
         timed_wall_s=t_all)
     print(json.dumps(line), flush=True)
     return 0
+
+
+class _SampledWeightedTasks:
+    """Load-balancer view whose task() applies SSF weights (CPU oracle) on
+    demand, so that only the tasks a CPU sample touches are weighted."""
+
+    def __init__(self, lb, mol):
+        self.lb, self.coords, self.cache = lb, mol.coords(), {}
+
+    def ntasks(self):
+        return self.lb.ntasks()
+
+    def task_info(self, i):
+        return self.lb.task_info(i)
+
+    def task(self, i):
+        if i not in self.cache:
+            import oracle
+            t = dict(self.lb.task(i))
+            n = t["npts"]
+            t["weights"] = oracle.ssf_weights(t["points"], np.full(n, t["iParent"], np.int32),
+                                              np.full(n, t["dist_nearest"]), self.coords,
+                                              t["weights"])
+            self.cache[i] = t
+        return self.cache[i]
 
 
 class _WeightedTasks:
