@@ -11,7 +11,14 @@
 // blocks when gradients are requested.  Padding columns are written as zero.
 // One thread owns one point and walks the task's shell list, so every store
 // of a warp covers 32 consecutive points of one column.
+//
+// The value type is double for the FP64 path and a float-float pair (ff::ffl,
+// same 8-byte slots) for the point blocks of the tensor-core path, where the
+// digits need about 44 significant bits: FP32 instructions then replace the
+// FP64 ones of exp and of the angular polynomials, GB300's FP64 pipe being
+// about 64 times slower than its FP32 pipe.
 #include "device_common.cuh"
+#include "ffmath.cuh"
 #include "xc_mixed.cuh"
 #include "collocation_angular.inc"
 
@@ -19,10 +26,9 @@ namespace gb300 {
 
 namespace {
 
-template <bool GRAD>
-__device__ __forceinline__ void eval_shell(int l, int pure, double x, double y, double z, double R,
-                                           double R1, double* f, double* fx, double* fy,
-                                           double* fz, int64_t s) {
+template <bool GRAD, typename V>
+__device__ __forceinline__ void eval_shell(int l, int pure, V x, V y, V z, V R, V R1, V* f, V* fx,
+                                           V* fy, V* fz, int64_t s) {
   if (GRAD) {
     if (pure) {
       switch (l) {
@@ -65,7 +71,11 @@ __device__ __forceinline__ void eval_shell(int l, int pure, double x, double y, 
 // With MASK, a block of merged tasks is evaluated on its union shell list and
 // a shell outside the point's own task list contributes exact zeros, so the
 // merged block reproduces the per-task screening of the reference.
-template <bool GRAD, bool MASK>
+// exp(-a r2) in the value type's arithmetic
+__device__ __forceinline__ double exp_neg_v(double x) { return exp(x); }
+__device__ __forceinline__ ff::ffl exp_neg_v(ff::ffl x) { return ff::exp_neg(x); }
+
+template <bool GRAD, bool MASK, typename V>
 __global__ void __launch_bounds__(128) collocation_kernel(ShellsDev sh, TasksDev tk, PBMaskDev mk,
                                                           const int2* __restrict__ items,
                                                           double* __restrict__ scr) {
@@ -75,13 +85,14 @@ __global__ void __launch_bounds__(128) collocation_kernel(ShellsDev sh, TasksDev
   const int np = tk.npts_pad[t];
   if (p >= np) return;
   const int64_t g = tk.pt_off[t] + p;
-  const double px = tk.x[g], py = tk.y[g], pz = tk.z[g];
+  const V px = V(tk.x[g]), py = V(tk.y[g]), pz = V(tk.z[g]);
   const int64_t ld = np;
   const int64_t blk = (int64_t)np * tk.nbe_pad[t];
-  double* f = scr + tk.scr_off[t];
-  double* fx = f + blk;
-  double* fy = fx + blk;
-  double* fz = fy + blk;
+  V* f = reinterpret_cast<V*>(scr + tk.scr_off[t]);
+  V* fx = f + blk;
+  V* fy = fx + blk;
+  V* fz = fy + blk;
+  const V zero = V(0);
   const int64_t s0 = tk.sh_off[t];
   const int ns = tk.nsh[t];
   const uint8_t* active = nullptr;
@@ -93,37 +104,37 @@ __global__ void __launch_bounds__(128) collocation_kernel(ShellsDev sh, TasksDev
       const int sz = sh.pure[s] ? 2 * sh.l[s] + 1 : (sh.l[s] + 1) * (sh.l[s] + 2) / 2;
       for (int m = 0; m < sz; ++m) {
         const int64_t o = (int64_t)(col + m) * ld + p;
-        f[o] = 0.;
+        f[o] = zero;
         if (GRAD) {
-          fx[o] = 0.;
-          fy[o] = 0.;
-          fz[o] = 0.;
+          fx[o] = zero;
+          fy[o] = zero;
+          fz[o] = zero;
         }
       }
       continue;
     }
-    const double dx = px - sh.origin[3 * s + 0];
-    const double dy = py - sh.origin[3 * s + 1];
-    const double dz = pz - sh.origin[3 * s + 2];
-    const double r2 = dx * dx + dy * dy + dz * dz;
-    double R = 0., R1 = 0.;
+    const V dx = px - V(sh.origin[3 * s + 0]);
+    const V dy = py - V(sh.origin[3 * s + 1]);
+    const V dz = pz - V(sh.origin[3 * s + 2]);
+    const V r2 = dx * dx + dy * dy + dz * dz;
+    V R = zero, R1 = zero;
     for (int k = sh.prim_off[s]; k < sh.prim_off[s + 1]; ++k) {
-      const double a = sh.alpha[k];
-      const double e = sh.coeff[k] * exp(-a * r2);
-      R += e;
-      if (GRAD) R1 += a * e;
+      const V a = V(sh.alpha[k]);
+      const V e = V(sh.coeff[k]) * exp_neg_v(-(a * r2));
+      R = R + e;
+      if (GRAD) R1 = R1 + a * e;
     }
-    R1 *= -2.;
+    R1 = R1 * V(-2);
     const int64_t o = (int64_t)col * ld + p;
     eval_shell<GRAD>(sh.l[s], sh.pure[s], dx, dy, dz, R, R1, f + o, fx + o, fy + o, fz + o, ld);
   }
   for (int c = tk.nbe[t]; c < tk.nbe_pad[t]; ++c) {
     const int64_t o = (int64_t)c * ld + p;
-    f[o] = 0.;
+    f[o] = zero;
     if (GRAD) {
-      fx[o] = 0.;
-      fy[o] = 0.;
-      fz[o] = 0.;
+      fx[o] = zero;
+      fy[o] = zero;
+      fz[o] = zero;
     }
   }
 }
@@ -135,9 +146,9 @@ void launch_collocation(const ShellsDev& sh, const TasksDev& tk, const int2* ite
   if (nitems == 0) return;
   const PBMaskDev none{};
   if (grad)
-    collocation_kernel<true, false><<<nitems, 128, 0, s>>>(sh, tk, none, items, scr);
+    collocation_kernel<true, false, double><<<nitems, 128, 0, s>>>(sh, tk, none, items, scr);
   else
-    collocation_kernel<false, false><<<nitems, 128, 0, s>>>(sh, tk, none, items, scr);
+    collocation_kernel<false, false, double><<<nitems, 128, 0, s>>>(sh, tk, none, items, scr);
   GB300_CUDA(cudaGetLastError());
 }
 
@@ -146,9 +157,9 @@ void launch_collocation_masked(const ShellsDev& sh, const TasksDev& tk, const PB
                                cudaStream_t s) {
   if (nitems == 0) return;
   if (grad)
-    collocation_kernel<true, true><<<nitems, 128, 0, s>>>(sh, tk, mk, items, scr);
+    collocation_kernel<true, true, ff::ffl><<<nitems, 128, 0, s>>>(sh, tk, mk, items, scr);
   else
-    collocation_kernel<false, true><<<nitems, 128, 0, s>>>(sh, tk, mk, items, scr);
+    collocation_kernel<false, true, ff::ffl><<<nitems, 128, 0, s>>>(sh, tk, mk, items, scr);
   GB300_CUDA(cudaGetLastError());
 }
 

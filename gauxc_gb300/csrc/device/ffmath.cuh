@@ -33,6 +33,32 @@ __device__ __forceinline__ long long fixed42(double v, int es) {
   return (b >> 63) ? -q : q;
 }
 
+// BF16 bit pattern of d * 2^(-7 i) for an integer |d| <= 255, i <= 5, by
+// integer operations: d becomes an exact float through the 1.5 * 2^23 bias,
+// its top 16 bits are the exact BF16 (at most 8 significant bits), and 7 i is
+// taken off the exponent field (never below 1 for these ranges).
+__device__ __forceinline__ unsigned bf16_digit(int d, int i) {
+  const float f = __int_as_float(0x4B400000 + d) - 12582912.f;
+  const unsigned b = __float_as_uint(f) >> 16;
+  return d ? b - ((unsigned)(7 * i) << 7) : 0u;
+}
+
+// Balanced base-128 digits of q (|q| <= 2^42) as BF16 bit patterns of
+// d_i * 2^(-7 i), d_0 in [-128, 128], the others in [-64, 63].
+template <int S, typename Store>
+__device__ __forceinline__ void digits_bf16(long long q, Store&& store) {
+  int d[S];
+#pragma unroll
+  for (int i = S - 1; i > 0; --i) {
+    const int di = (int)((q + 64) & 127) - 64;
+    d[i] = di;
+    q = (q - di) >> 7;
+  }
+  d[0] = (int)q;
+#pragma unroll
+  for (int i = 0; i < S; ++i) store(i, bf16_digit(d[i], i));
+}
+
 // Balanced base-128 digits of q (|q| <= 2^42): q = sum_i d_i 128^(S-1-i),
 // d_0 in [-128, 128], others in [-64, 63].  Writes d_i * 2^(-7 i) (exact in bf16).
 template <int S, typename Store>
@@ -163,6 +189,110 @@ __device__ __forceinline__ float2 add(float2 a, float2 b) {
   float s, e;
   two_sum(a.x, b.x, s, e);
   return make_float2(s, a.y + b.y + e);
+}
+
+// ---------------------------------------------------------------- float-float type
+// Unevaluated sum hi + lo of two floats (about 46 significant bits), with the
+// arithmetic the generated collocation templates use.  Device code builds
+// values from doubles by bit manipulation (no FP64 instructions).
+struct ffl {
+  float hi, lo;
+  ffl() = default;
+  __host__ __device__ constexpr ffl(float h, float l) : hi(h), lo(l) {}
+  __host__ __device__ ffl(double v) {
+#ifdef __CUDA_ARCH__
+    const float2 t = split(v);
+    hi = t.x;
+    lo = t.y;
+#else
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+#endif
+  }
+  __host__ __device__ ffl(int v) : ffl((double)v) {}
+};
+
+// s + e = a + b for |a| >= |b| (or a == 0)
+__host__ __device__ __forceinline__ ffl fast_two_sum(float a, float b) {
+  const float s = a + b;
+  return ffl(s, b - (s - a));
+}
+__host__ __device__ __forceinline__ ffl operator+(ffl a, ffl b) {
+  const float s = a.hi + b.hi;
+  const float bb = s - a.hi;
+  const float e = (a.hi - (s - bb)) + (b.hi - bb);
+  return fast_two_sum(s, e + a.lo + b.lo);
+}
+__host__ __device__ __forceinline__ ffl operator-(ffl a) { return ffl(-a.hi, -a.lo); }
+__host__ __device__ __forceinline__ ffl operator-(ffl a, ffl b) { return a + (-b); }
+__host__ __device__ __forceinline__ ffl operator*(ffl a, ffl b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  return fast_two_sum(p, e);
+}
+__host__ __device__ __forceinline__ ffl& operator+=(ffl& a, ffl b) { return a = a + b; }
+__host__ __device__ __forceinline__ ffl& operator*=(ffl& a, ffl b) { return a = a * b; }
+
+// exp(x) for a float-float x <= 0, about 2^-45 relative; 0 below e^-87.
+// Method: k = rint(x / ln 2), r = x - k ln 2 with ln 2 split into three floats
+// (Cody-Waite: the first has 12 significant bits, so k times it is exact),
+// exp(r / 8) by its Taylor series to degree 9 (|r / 8| <= 0.044, truncation
+// below 2^-66), three squarings, then the exact scaling by 2^k.
+__device__ __forceinline__ ffl exp_neg(ffl x) {
+  if (x.hi < -87.f) return ffl(0.f, 0.f);
+  const float k = rintf(x.hi * 1.44269504088896341f);
+  const float c1 = 0.693115234375f, c2 = 3.194618329871446e-05f, c3 = 1.6465949697480609e-12f;
+  ffl r = x + ffl(-k * c1, 0.f);                 // k c1 exact
+  const float p2 = k * c2;
+  r = r + ffl(-p2, -fmaf(k, c2, -p2));           // k c2 as an exact product pair
+  r = r + ffl(-k * c3, 0.f);
+  const ffl t = r * ffl(0.125f, 0.f);
+  // Horner: sum_{n <= 9} t^n / n!
+  ffl y(2.7557319223985893e-06);                 // 1/9!
+  y = y * t + ffl(2.48015873015873e-05);         // 1/8!
+  y = y * t + ffl(1.984126984126984e-04);        // 1/7!
+  y = y * t + ffl(1.388888888888889e-03);        // 1/6!
+  y = y * t + ffl(8.333333333333333e-03);        // 1/5!
+  y = y * t + ffl(4.1666666666666664e-02);       // 1/4!
+  y = y * t + ffl(1.6666666666666666e-01);       // 1/3!
+  y = y * t + ffl(0.5f, 0.f);
+  y = y * t + ffl(1.f, 0.f);
+  y = y * t + ffl(1.f, 0.f);
+  y = y * y;
+  y = y * y;
+  y = y * y;
+  const int ki = (int)k;
+  const float s = ki >= -126 ? __uint_as_float((unsigned)(ki + 127) << 23) : 0.f;
+  return ffl(y.hi * s, y.lo * s);
+}
+
+// q = round(v * 2^(42 - es)) for a float v with |v| < 2^es, by shifting the mantissa.
+__device__ __forceinline__ long long fixed42f(float v, int es) {
+  const unsigned b = __float_as_uint(v);
+  const int E = (int)((b >> 23) & 0xFF);
+  if (E == 0) return 0;
+  const long long mant = (long long)((b & 0x7FFFFFu) | 0x800000u);
+  const int sh = E - 150 + 42 - es;  // v * 2^(42 - es) = mant * 2^sh
+  long long q;
+  if (sh >= 0)
+    q = sh > 38 ? 0 : mant << sh;  // |v| < 2^es keeps q below 2^42
+  else
+    q = -sh > 62 ? 0 : (mant + (1LL << (-sh - 1))) >> (-sh);
+  return (b >> 31) ? -q : q;
+}
+
+// q = round(v * 2^(42 - es)) for a float-float v (|v| < 2^es)
+__device__ __forceinline__ long long fixed42(ffl v, int es) {
+  return fixed42f(v.hi, es) + fixed42f(v.lo, es);
+}
+
+// Power-of-two exponent e with |x| < 2^e for the largest |hi| of float-float
+// values, given as the float magnitude bits of that hi (0 gives -126).
+__device__ __forceinline__ int scale_exponent_f(unsigned key) {
+  const int E = (int)(key >> 23);
+  return E == 0 ? -126 : E - 126;
 }
 
 }  // namespace ff

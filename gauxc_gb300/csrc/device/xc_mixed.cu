@@ -25,15 +25,15 @@ __device__ __forceinline__ int exp_of_pow2(double p) {
   return (int)(((unsigned long long)__double_as_longlong(p) >> 52) & 0x7FF) - 1023;
 }
 
-// Digits of 8 values x[e] (|x[e]| < 2^es[e]) stored as kSlices 16-byte rows:
-// plane i at out + i * plane.
-__device__ __forceinline__ void store_digits8(const double (&x)[8], const int (&es)[8],
+// Digits of 8 values x[e] (|x[e]| < 2^es[e]; double or float-float) stored as
+// kSlices 16-byte rows: plane i at out + i * plane.
+template <typename T>
+__device__ __forceinline__ void store_digits8(const T (&x)[8], const int (&es)[8],
                                               __nv_bfloat16* out, int64_t plane) {
   uint32_t w[kSlices][4];
 #pragma unroll
   for (int e = 0; e < 8; ++e)
-    ff::digits<kSlices>(ff::fixed42(x[e], es[e]), [&](int i, float dv) {
-      const uint32_t h = __bfloat16_as_ushort(__float2bfloat16_rn(dv));
+    ff::digits_bf16<kSlices>(ff::fixed42(x[e], es[e]), [&](int i, unsigned h) {
       if (e & 1)
         w[i][e >> 1] |= h << 16;
       else
@@ -44,22 +44,32 @@ __device__ __forceinline__ void store_digits8(const double (&x)[8], const int (&
     __stcs(reinterpret_cast<uint4*>(out + i * plane), make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]));
 }
 
+using ff::ffl;
+
+// float-float scaled by 2^e (exact in the float range)
+__device__ __forceinline__ ffl scale2(ffl v, int e) {
+  const float s = ff::pow2f(e);
+  return ffl(v.hi * s, v.lo * s);
+}
+
+__device__ __forceinline__ unsigned abs_key_f(ffl v) { return __float_as_uint(v.hi) & 0x7FFFFFFFu; }
+
 struct PBView {
   PBDims d;
   PBF64 o;
-  const double* phi;
+  const ffl* phi;            // [q][mu][p], float-float (collocation of the point blocks)
   double *r, *sp, *cz;
-  unsigned long long* gkey;  // largest |grad phi| of each point, as abs_key
+  unsigned* gkey;            // largest |grad phi| of each point, as float magnitude bits
   float2* phi2;              // [q][p][mu]
   __nv_bfloat16 *Pd, *Fd, *Va, *Vb;
   __device__ PBView(const TasksDev& tk, const MixedPBDev& mp, int b, bool gga, const double* f64c,
                     const __nv_bfloat16* digc)
       : d(tk.npts_pad[b], tk.nbe[b]), o(d, gga ? 4 : 1) {
     double* base = const_cast<double*>(f64c) + mp.f64_off[b];
-    phi = base;
+    phi = reinterpret_cast<const ffl*>(base);
     r = base + o.r;
     sp = base + o.sp;
-    gkey = reinterpret_cast<unsigned long long*>(base + o.gp);
+    gkey = reinterpret_cast<unsigned*>(base + o.gp);
     cz = base + o.cz;
     phi2 = reinterpret_cast<float2*>(base + o.phi2);
     __nv_bfloat16* dg = digc ? const_cast<__nv_bfloat16*>(digc) + mp.dig_off[b] : nullptr;
@@ -91,10 +101,10 @@ __global__ void point_scale_kernel(TasksDev tk, MixedPBDev mp, int b0, double* f
   const int b = b0 + blockIdx.y;
   PBView v(tk, mp, b, gga, f64, nullptr);
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < v.d.np; p += gridDim.x * blockDim.x) {
-    unsigned long long m = 0;
-    for (int mu = 0; mu < v.d.nu; ++mu) m = max(m, ff::abs_key(v.phi[(int64_t)mu * v.d.np + p]));
-    v.sp[p] = ff::pow2(ff::scale_exponent(m));
-    v.gkey[p] = 0ULL;
+    unsigned m = 0;
+    for (int mu = 0; mu < v.d.nu; ++mu) m = max(m, abs_key_f(v.phi[(int64_t)mu * v.d.np + p]));
+    v.sp[p] = ff::pow2(ff::scale_exponent_f(m));
+    v.gkey[p] = 0u;
   }
 }
 
@@ -114,14 +124,14 @@ __global__ void phi_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const doub
   const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
   for (int u = t0; u < d.nu128 * (d.np / 8); u += stride) {
     const int mu = u % d.nu128, p0 = (u / d.nu128) * 8;
-    double x[8];
+    ffl x[8];
     int es[8];
-    const double2* src = reinterpret_cast<const double2*>(v.phi + (int64_t)mu * d.np + p0);
+    const float4* src = reinterpret_cast<const float4*>(v.phi + (int64_t)mu * d.np + p0);
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
-      const double2 t = src[e];
-      x[2 * e] = t.x;
-      x[2 * e + 1] = t.y;
+      const float4 t = src[e];
+      x[2 * e] = ffl(t.x, t.y);
+      x[2 * e + 1] = ffl(t.z, t.w);
     }
 #pragma unroll
     for (int e = 0; e < 8; ++e) es[e] = exp_of_pow2(v.sp[p0 + e]);
@@ -133,19 +143,17 @@ __global__ void phi_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const doub
   const int ng = d.nu128 / 8;
   const int per = (ng + gridDim.x - 1) / gridDim.x;
   const int g0 = blockIdx.x * per, g1 = min(ng, g0 + per);
-  unsigned long long gmax = 0;
+  unsigned gmax = 0;
   for (int g = g0; g < g1; ++g) {
     const int mu0 = g * 8;
     for (int q = 0; q < nq; ++q) {
-      double x[8];
+      ffl x[8];
 #pragma unroll
       for (int e = 0; e < 8; ++e) x[e] = v.phi[q * v.o.blk + (int64_t)(mu0 + e) * d.np + p];
       float4* dst = reinterpret_cast<float4*>(v.phi2 + q * v.o.blk + (int64_t)p * d.nu128 + mu0);
 #pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const float2 a = ff::split(x[2 * e]), c = ff::split(x[2 * e + 1]);
-        dst[e] = make_float4(a.x, a.y, c.x, c.y);
-      }
+      for (int e = 0; e < 4; ++e)
+        dst[e] = make_float4(x[2 * e].hi, x[2 * e].lo, x[2 * e + 1].hi, x[2 * e + 1].lo);
       if (q == 0 && mu0 < d.nu16) {
         int es[8];
         const int e0 = exp_of_pow2(v.sp[p]);
@@ -155,7 +163,7 @@ __global__ void phi_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const doub
       }
       if (q > 0)
 #pragma unroll
-        for (int e = 0; e < 8; ++e) gmax = max(gmax, ff::abs_key(x[e]));
+        for (int e = 0; e < 8; ++e) gmax = max(gmax, abs_key_f(x[e]));
     }
   }
   if (gga && gmax) atomicMax(v.gkey + p, gmax);
@@ -222,8 +230,8 @@ __global__ void p_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const double
 }
 
 // ---------------------------------------------------------------- Z digits
-// Zt[nu][p] = sp[p] (zc.x phi + zc.y dphi_x + zc.z dphi_y + zc.w dphi_z) with
-// one scale cz for the whole block: 2^e above the bound
+// Zt[nu][p] = sp[p] (zc.x phi + zc.y dphi_x + zc.z dphi_y + zc.w dphi_z),
+// in float-float, with one scale cz for the whole block: 2^e above the bound
 //   |Zt| <= sp (|zc.x| sp + (|zc.y| + |zc.z| + |zc.w|) max|grad phi|)
 // taken from exponents only.  Digits go to Vb[nu][p] (rows nu < nun) and
 // Va[nu][np + p] (rows nu < nu128).  One CTA per 8 rows nu; thread (row
@@ -235,18 +243,18 @@ __global__ void z_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const double
   PBView v(tk, mp, b, gga, f64, dig);
   const PBDims& d = v.d;
   if (blockIdx.x * 8 >= d.nu128) return;
-  const double4* z = zc + tk.pt_off[b];
+  // coefficients of point p: zf[4 p + k], float-float (functional_kernel)
+  const ffl* zf = reinterpret_cast<const ffl*>(zc + tk.pt_off[b]);
   // block scale: max over points of the exponent bound
   int eb = -1000;
   for (int p = threadIdx.x; p < d.np; p += blockDim.x) {
-    const double4 c = z[p];
     const int esp = exp_of_pow2(v.sp[p]);
-    int t = ff::scale_exponent(ff::abs_key(c.x)) + esp;
+    int t = ff::scale_exponent_f(abs_key_f(zf[4 * p])) + esp;
     if (gga) {
-      const int eg = ff::scale_exponent(v.gkey[p]);
-      t = max(t, ff::scale_exponent(ff::abs_key(c.y)) + eg);
-      t = max(t, ff::scale_exponent(ff::abs_key(c.z)) + eg);
-      t = max(t, ff::scale_exponent(ff::abs_key(c.w)) + eg);
+      const int eg = ff::scale_exponent_f(v.gkey[p]);
+      t = max(t, ff::scale_exponent_f(abs_key_f(zf[4 * p + 1])) + eg);
+      t = max(t, ff::scale_exponent_f(abs_key_f(zf[4 * p + 2])) + eg);
+      t = max(t, ff::scale_exponent_f(abs_key_f(zf[4 * p + 3])) + eg);
       t += 2;
     }
     eb = max(eb, t + esp);
@@ -261,18 +269,20 @@ __global__ void z_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const double
   if (threadIdx.x < 8) v.cz[row] = ff::pow2(es_z);
   const int ng = d.np / 8, step = blockDim.x / 8;
   const int k2 = 2 * d.np;
-  const double* f = v.phi + (int64_t)row * d.np;
+  const ffl* f = v.phi + (int64_t)row * d.np;
+  // Zt in float-float; the point scale is an exact power of two
   auto zval = [&](int p) {
-    const double4 c = z[p];
-    double val = c.x * f[p];
-    if (gga) val += c.y * f[p + v.o.blk] + c.z * f[p + 2 * v.o.blk] + c.w * f[p + 3 * v.o.blk];
-    return v.sp[p] * val;
+    ffl val = zf[4 * p] * f[p];
+    if (gga)
+      val = val + zf[4 * p + 1] * f[p + v.o.blk] + zf[4 * p + 2] * f[p + 2 * v.o.blk] +
+            zf[4 * p + 3] * f[p + 3 * v.o.blk];
+    return scale2(val, exp_of_pow2(v.sp[p]));
   };
   int es[8];
 #pragma unroll
   for (int e = 0; e < 8; ++e) es[e] = es_z;
   for (int g = threadIdx.x >> 3; g < ng; g += step) {
-    double x[8];
+    ffl x[8];
 #pragma unroll
     for (int e = 0; e < 8; ++e) x[e] = zval(g * 8 + e);
     store_digits8(x, es, v.Va + oz_offset(0, row, d.np + g * 8, kMTile, k2), kMTile * kBK);
@@ -297,8 +307,14 @@ __global__ void functional_kernel(int64_t g0, int64_t g1, const double* __restri
     e += (wg * eps) * r;
     n += wg * r;
     const double gf = 2. * wg * vs;
-    zcoef[g] = func.is_gga ? make_double4(0.5 * wg * vr, gf * dx, gf * dy, gf * dz)
-                           : make_double4(0.5 * wg * vr, 0., 0., 0.);
+    // Z coefficients for z_digits_kernel as four float-float pairs in the
+    // point's 32-byte slot
+    const double c0 = 0.5 * wg * vr, c1 = func.is_gga ? gf * dx : 0.,
+                 c2 = func.is_gga ? gf * dy : 0., c3 = func.is_gga ? gf * dz : 0.;
+    const float2 a = ff::split(c0), b = ff::split(c1), c = ff::split(c2), e = ff::split(c3);
+    float4* zq = reinterpret_cast<float4*>(zcoef + g);
+    zq[0] = make_float4(a.x, a.y, b.x, b.y);
+    zq[1] = make_float4(c.x, c.y, e.x, e.y);
   }
   se[threadIdx.x] = e;
   sn[threadIdx.x] = n;
