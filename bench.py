@@ -336,6 +336,7 @@ def run_batched(args, dist, rank, local, ncores):
                  d2h_bytes_per_step=int(sum(n * n * 8 + 16 for n in nbfs)), pinned=True),
         roofline=roofline, cpu_baseline=cpu, gpu_launches=launches,
         graph_launches_per_step=1, clocks=clocks, fp64_check=fp64_check, autotune=tune,
+        grid_points_bf_per_s=sum(st["sum_npts_nbe"] for st in stats) / value,
         exc_sum=float(np.sum(exc)),
         setup_s=dict(load_balancer=t_lb, ssf_weights=t_w), timed_wall_s=t_all)
     print(json.dumps(line), flush=True)
@@ -532,6 +533,7 @@ def main():
         roofline=roofline, cpu_baseline=cpu, gpu_launches=launches, clocks=clocks,
         fp64_check=fp64_check,
         exc=exc, nel=integ.last_nel(),
+        grid_points_bf_per_s=stats["sum_npts_nbe"] / value,
         kernels={k: dict(ms_per_step=v["ms"] / args.steps, launches_per_step=v["launches"] / args.steps)
                  for k, v in kt.items()},
         setup_s=dict(load_balancer=ctx["t_lb"], ssf_weights=ctx["t_w"]),
