@@ -544,9 +544,10 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
     cur.max_nu_pad = std::max(cur.max_nu_pad, nu_pad[i]);
     for (int b = 0; b < (npts_pad[i] + 127) / 128; ++b) coll.push_back(make_int2(i, b));
     const PBDims d(npts_pad[i], nu[i]);
+    // tiles of one A row block and K chunk next to each other (they share A)
     for (int m0 = 0; m0 < d.nu128; m0 += kMTile)
-      for (int n0 = 0; n0 < d.np; n0 += kNTile)
-        for (int k0 = 0; k0 < d.nu16; k0 += kMaxK)
+      for (int k0 = 0; k0 < d.nu16; k0 += kMaxK)
+        for (int n0 = 0; n0 < d.np; n0 += kNTile)
           xi.push_back(OzItem{i, m0, n0, k0, std::min(k0 + kMaxK, d.nu16)});
     // symmetric VXC: tiles reaching the upper triangle, K = phi | Z
     for (int m0 = 0; m0 < d.nu128; m0 += kMTile)

@@ -426,30 +426,42 @@ int ozaki_schedule(std::vector<OzItem>& items, size_t begin, size_t end, int nsm
     cta_off.push_back((int)begin);
     return 0;
   }
+  // Gangs of kGang CTAs take slots of kGang consecutive tiles (the list holds
+  // the tiles of one operand row next to each other, so a slot's tiles share
+  // their A operand); member j of the gang gets tile j of each of its slots.
+  // The members start together and run tiles of equal K, so they stream the
+  // same A blocks at about the same time and all but the first read hit L2.
+  // Slots go, in list order (point blocks in atom order), to the least loaded
+  // gang.
+  constexpr int kGang = 4;
   const int ncta = (int)std::min<size_t>((size_t)std::max(nsm, 1), n);
-  // cost of a tile in K blocks, plus a fixed share for its epilogue
+  const int g = ncta >= kGang ? kGang : 1;
+  const int ngang = ncta / g;  // every CTA gets at least one tile (n >= ncta)
   auto cost = [](const OzItem& q) { return (q.k1 - q.k0) / kBK + 2; };
-  // tiles keep their list order (point blocks in atom order), so the CTAs
-  // advance through the atoms together and their output updates share L2
   const std::vector<OzItem> v(items.begin() + begin, items.begin() + end);
   using Load = std::pair<long long, int>;
   std::priority_queue<Load, std::vector<Load>, std::greater<Load>> heap;
-  for (int c = 0; c < ncta; ++c) heap.push({0LL, c});
-  std::vector<std::vector<OzItem>> lists(ncta);
-  for (const OzItem& q : v) {
+  for (int c = 0; c < ngang; ++c) heap.push({0LL, c});
+  const int nused = ngang * g;
+  std::vector<std::vector<OzItem>> lists(nused);
+  for (size_t s0 = 0; s0 < v.size(); s0 += g) {
     Load l = heap.top();
     heap.pop();
-    lists[l.second].push_back(q);
-    l.first += cost(q);
+    long long c = 0;
+    for (int k = 0; k < g && s0 + k < v.size(); ++k) {
+      lists[l.second * g + k].push_back(v[s0 + k]);
+      c = std::max<long long>(c, cost(v[s0 + k]));
+    }
+    l.first += c;
     heap.push(l);
   }
   size_t at = begin;
-  for (int c = 0; c < ncta; ++c) {
+  for (int c = 0; c < nused; ++c) {
     cta_off.push_back((int)at);
     for (const OzItem& q : lists[c]) items[at++] = q;
   }
   cta_off.push_back((int)at);
-  return ncta;
+  return nused;
 }
 
 // Self-test of the symmetric VXC GEMM: S = F Z^T + Z F^T (n x n) over k

@@ -140,8 +140,8 @@ void launch_ozaki_v(const TasksDev& tk, const MixedPBDev& mp, const OzSchedule& 
                     int* err, cudaStream_t s);
 
 // Host: order items[begin, end) into per-CTA lists for a persistent launch on
-// `nsm` CTAs (each tile, in list order, onto the least loaded CTA); appends
-// ncta + 1 absolute offsets to cta_off and returns ncta.
+// up to `nsm` CTAs (gangs of CTAs take slots of consecutive tiles, see
+// ozaki_gemm.cu); appends ncta + 1 absolute offsets to cta_off and returns ncta.
 int ozaki_schedule(std::vector<OzItem>& items, size_t begin, size_t end, int nsm,
                    std::vector<int>& cta_off);
 
