@@ -92,8 +92,8 @@ struct MBatch {
   int64_t g0, g1;            // point range
   int max_nu_pad;
   int partial_base;
-  int x_sched, x_ncta;       // persistent-launch schedules (offsets into sched_)
-  int v_sched, v_ncta;
+  int x_sched, x_ncl;        // persistent-launch schedules (offsets into sched_, clusters)
+  int v_sched, v_ncl;
 };
 
 }  // namespace
@@ -167,8 +167,7 @@ class DeviceIntegrator {
   PBMaskDev mk_{};
   MixedPBDev mp_{};
   std::vector<MBatch> mbatches_;
-  OzItem* x_items_ = nullptr;
-  OzItem* v_items_ = nullptr;
+  OzItem* slots_ = nullptr;  // GEMM slots of every launch (kCluster tiles each)
   int* sched_ = nullptr;
   double* f64_ = nullptr;
   __nv_bfloat16* dig_ = nullptr;
@@ -544,11 +543,15 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
     cur.max_nu_pad = std::max(cur.max_nu_pad, nu_pad[i]);
     for (int b = 0; b < (npts_pad[i] + 127) / 128; ++b) coll.push_back(make_int2(i, b));
     const PBDims d(npts_pad[i], nu[i]);
-    // tiles of one A row block and K chunk next to each other (they share A)
-    for (int m0 = 0; m0 < d.nu128; m0 += kMTile)
-      for (int k0 = 0; k0 < d.nu16; k0 += kMaxK)
-        for (int n0 = 0; n0 < d.np; n0 += kNTile)
-          xi.push_back(OzItem{i, m0, n0, k0, std::min(k0 + kMaxK, d.nu16)});
+    // tiles of one A row block and K chunk next to each other (they share
+    // A); the full-length K chunks first, so that a cluster slot rarely
+    // mixes tiles of different K
+    const int nfull = d.nu16 / kMaxK, nchunk = (d.nu16 + kMaxK - 1) / kMaxK;
+    for (int pass = 0; pass < 2; ++pass)
+      for (int m0 = 0; m0 < d.nu128; m0 += kMTile)
+        for (int c = pass ? nfull : 0; c < (pass ? nchunk : nfull); ++c)
+          for (int n0 = 0; n0 < d.np; n0 += kNTile)
+            xi.push_back(OzItem{i, m0, n0, c * kMaxK, std::min((c + 1) * kMaxK, d.nu16)});
     // symmetric VXC: tiles reaching the upper triangle, K = phi | Z
     for (int m0 = 0; m0 < d.nu128; m0 += kMTile)
       for (int n0 = 0; n0 < d.nun; n0 += kNTile)
@@ -563,16 +566,15 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
     for (const OzItem& q : xi) stats.tensor_flops_x += 2.0 * kMTile * kNTile * (q.k1 - q.k0) * npairs;
     for (const OzItem& q : vi) stats.tensor_flops_v += 2.0 * kMTile * kNTile * (q.k1 - q.k0) * npairs;
   }
-  // per-CTA tile lists of every persistent GEMM launch
-  int nsm = 0, dev = 0;
-  GB300_CUDA(cudaGetDevice(&dev));
-  GB300_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  // per-cluster slot lists of every persistent GEMM launch
+  const int ncl = ozaki_clusters();
   std::vector<int> sched;
+  std::vector<OzItem> slots;
   for (MBatch& mb : mbatches_) {
     mb.x_sched = (int)sched.size();
-    mb.x_ncta = ozaki_schedule(xi, mb.x_begin, mb.x_end, nsm, sched);
+    mb.x_ncl = ozaki_schedule(xi, mb.x_begin, mb.x_end, ncl, slots, sched);
     mb.v_sched = (int)sched.size();
-    mb.v_ncta = ozaki_schedule(vi, mb.v_begin, mb.v_end, nsm, sched);
+    mb.v_ncl = ozaki_schedule(vi, mb.v_begin, mb.v_end, ncl, slots, sched);
   }
   stats.nbatches = (int64_t)mbatches_.size();
   stats.scratch_bytes = max_f64 + max_dig;
@@ -599,8 +601,7 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
   mp_.f64_off = tk_.scr_off;
   mp_.dig_off = arena_.upload(dig_off, s);
   coll_items_ = arena_.upload(coll, s);
-  x_items_ = arena_.upload(xi, s);
-  v_items_ = arena_.upload(vi, s);
+  slots_ = arena_.upload(slots, s);
   sched_ = arena_.upload(sched, s);
   f64_ = arena_.alloc<double>((size_t)(max_f64 / 8.) + 32);
   dig_ = arena_.alloc<__nv_bfloat16>((size_t)(max_dig / 2.) + 128);
@@ -632,7 +633,7 @@ int64_t DeviceIntegrator::eval_mixed_batches(bool do_vxc) {
       return (int64_t)3;
     });
     launches += timed(1, [&] {
-      launch_ozaki_x(tk_, mp_, OzSchedule{x_items_, sched_ + b.x_sched, b.x_ncta}, f64_, dig_, gga_,
+      launch_ozaki_x(tk_, mp_, OzSchedule{slots_, sched_ + b.x_sched, b.x_ncl}, f64_, dig_, gga_,
                      rho4_, err_, s);
       return (int64_t)1;
     });
@@ -646,7 +647,7 @@ int64_t DeviceIntegrator::eval_mixed_batches(bool do_vxc) {
       return (int64_t)1;
     });
     launches += timed(3, [&] {
-      launch_ozaki_v(tk_, mp_, OzSchedule{v_items_, sched_ + b.v_sched, b.v_ncta}, f64_, dig_, gga_,
+      launch_ozaki_v(tk_, mp_, OzSchedule{slots_, sched_ + b.v_sched, b.v_ncl}, f64_, dig_, gga_,
                      A_, nbf_, err_, s);
       return (int64_t)1;
     });

@@ -12,13 +12,22 @@
 //    run, and A[mu, nu] += 2^-14 cz D for mu < nu (half of it for mu = nu),
 //    scattered with coalesced FP64 atomics.
 //
-// Persistent, warp-specialised CTAs (one per SM), each walking its own list
-// of tiles (128 x 64 outputs):
-//   warp 0    producer: two bulk copies per K block (the operands are stored
-//             in HBM as shared-memory images, xc_mixed.cuh) into a kStages
-//             ring, completion counted on the stage's `full` mbarrier;
+// Persistent, warp-specialised CTAs (one per SM) in clusters of kCluster.  A
+// cluster walks a list of slots; a slot holds one tile (128 x 64 outputs) per
+// CTA of the cluster, or none.  Tiles of a slot with the same A operand
+// (point block, row block, K range) form a sharing group: each of its CTAs
+// loads 1/n of every A block and multicasts it to all n, so the group reads A
+// from memory once.  All CTAs of a cluster step through the same sequence of
+// stage uses (as many per slot as the slot's longest tile has K blocks) and
+// each MMA commit is multicast to the `empty` barrier of every CTA in the
+// cluster, so a producer refills a stage only when every CTA it writes to has
+// released it.
+//   warp 0    producer: per K block its share of A (multicast) and its own B
+//             tile as bulk copies (the operands are stored in HBM as
+//             shared-memory images, xc_mixed.cuh) into a kStages ring,
+//             completion counted on the stage's `full` mbarrier;
 //   warp 1    one lane issues the MMAs of a K block and commits them to the
-//             stage's `empty` mbarrier; after a tile's last block it commits
+//             stage's `empty` mbarriers; after a tile's last block it commits
 //             to `tfull`.  Each level i + j (0..5) of the slice-pair
 //             products has its own exact FP32 accumulator of 64 TMEM columns,
 //             placed so that digit plane i of A times adjacent B planes
@@ -31,8 +40,9 @@
 //             handed back (`tempty`) and the rest of the epilogue runs from
 //             registers while the next tile's MMAs proceed.
 // Every mbarrier wait is bounded.  On expiry the CTA records an error code,
-// each role leaves its loop, the producer waits (bounded) for its copies in
-// flight, the MMA lane for its MMAs, and TMEM is released.
+// each role leaves its loop, the producer waits (bounded) until the cluster
+// has released the stages it filled, the MMA lane for its MMAs, TMEM is
+// released and the CTAs of the cluster leave together.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -65,7 +75,9 @@ constexpr int kEpiStride = 17;  // padded row of a warp's 32 x 16 transposition 
 constexpr int kEpiBytes = kEpiWarps * 32 * kEpiStride * 8;
 constexpr int kBarOffset = kStages * kStageBytes + kEpiBytes;
 constexpr uint32_t kWaitLimit = 1u << 22;
+constexpr uint16_t kClusterMask = (1u << kCluster) - 1;
 static_assert(kBK == 16, "one MMA (K = 16) per operand tile");
+static_assert(kABytes % (16 * 12) == 0, "A shares of 1/2, 1/3, 1/4 are 16-byte multiples");
 static_assert(kNTile == 64 && kAccs * kNTile <= (int)kTmemCols, "six levels of 64 columns");
 static_assert(kSlices == 6 && kLevels == 7, "MMA grouping below assumes 6 digits, levels <= 7");
 
@@ -173,6 +185,42 @@ __device__ __forceinline__ void drain_levels(uint32_t tb, uint32_t col, float (&
   }
 }
 
+// A slot as seen by one CTA of the cluster: its tile (pb < 0: none), the
+// number of stage uses of the slot (K blocks of its longest tile), and the
+// CTAs sharing this CTA's A operand (mask; this CTA loads share `part` of
+// `nparts`).
+struct SlotView {
+  OzItem it;
+  int nkb, uses, part, nparts;
+  uint16_t mask;
+};
+
+__device__ __forceinline__ bool same_a(const OzItem& a, const OzItem& b) {
+  return a.pb == b.pb && a.m0 == b.m0 && a.k0 == b.k0 && a.k1 == b.k1;
+}
+
+__device__ __forceinline__ SlotView slot_view(const OzItem* items, int slot, int rank) {
+  OzItem q[kCluster];
+  SlotView v;
+#pragma unroll
+  for (int r = 0; r < kCluster; ++r) {
+    q[r] = items[(int64_t)slot * kCluster + r];
+    if (r == rank) v.it = q[r];
+  }
+  v.nkb = v.it.pb >= 0 ? (v.it.k1 - v.it.k0) / kBK : 0;
+  v.uses = 0;
+  v.mask = 0;
+#pragma unroll
+  for (int r = 0; r < kCluster; ++r) {
+    if (q[r].pb < 0) continue;
+    v.uses = max(v.uses, (q[r].k1 - q[r].k0) / kBK);
+    if (v.it.pb >= 0 && same_a(q[r], v.it)) v.mask |= (uint16_t)(1u << r);
+  }
+  v.part = __popc(v.mask & ((1u << rank) - 1));
+  v.nparts = __popc(v.mask);
+  return v;
+}
+
 // First element of the tile row block holding rows [m0, m0 + TR) of an
 // operand, for EPI's A (M) and B (N) operands.
 template <int EPI>
@@ -199,12 +247,14 @@ __global__ void __launch_bounds__(kThreads, 1)
                                              ~uintptr_t(1023));
   Bars* B = reinterpret_cast<Bars*>(smem + kBarOffset);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int beg = sched.cta_off[blockIdx.x], end = sched.cta_off[blockIdx.x + 1];
+  const int rank = (int)umma::cluster_ctarank();
+  const int cl = blockIdx.x / kCluster;
+  const int beg = sched.slot_off[cl], end = sched.slot_off[cl + 1];
 
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) {
       umma::mbar_init(&B->full[s], 1);
-      umma::mbar_init(&B->empty[s], 1);
+      umma::mbar_init(&B->empty[s], kCluster);  // one MMA commit from every CTA
     }
     umma::mbar_init(&B->tfull, 1);
     umma::mbar_init(&B->tempty, kEpiWarps);
@@ -215,57 +265,74 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (warp == 0) umma::tmem_alloc(&B->tmem_slot, kTmemCols);
   umma::fence_before_sync();
   __syncthreads();
+  // the barriers of every CTA are initialised before any peer copies or arrives
+  umma::cluster_sync();
   umma::fence_after_sync();
   const uint32_t tmem = B->tmem_slot;
 
   if (warp == 0) {
     // ------------------------------------------------------------ producer
     uint32_t g = 0;
-    for (int ii = beg; ii < end; ++ii) {
+    for (int sl = beg; sl < end; ++sl) {
       if (warp_failed(B)) break;
-      const OzItem it = sched.items[ii];
-      const __nv_bfloat16 *A, *Bm;
-      operands<EPI>(it, tk, mp, dig, A, Bm);
+      const SlotView v = slot_view(sched.items, sl, rank);
+      const uint8_t *A = nullptr, *Bm = nullptr;
+      if (v.nkb > 0) {
+        const __nv_bfloat16 *a, *b;
+        operands<EPI>(v.it, tk, mp, dig, a, b);
+        A = reinterpret_cast<const uint8_t*>(a) + (int64_t)(v.it.k0 / kBK) * kABytes;
+        Bm = reinterpret_cast<const uint8_t*>(b) + (int64_t)(v.it.k0 / kBK) * kBBytes;
+      }
+      const uint32_t a_lo = (uint32_t)(v.part * kABytes / max(v.nparts, 1));
+      const uint32_t a_hi = (uint32_t)((v.part + 1) * kABytes / max(v.nparts, 1));
       bool ok = true;
-      for (int kb = it.k0 / kBK; kb < it.k1 / kBK; ++kb) {
+      for (int u = 0; u < v.uses; ++u, ++g) {
         const int st = (int)(g % kStages);
+        // every CTA this one writes to has released the stage
         if (g >= (uint32_t)kStages && !warp_wait(&B->empty[st], ((g / kStages) - 1) & 1)) {
           if (lane == 0) set_fail(B, ERR_EMPTY);
           ok = false;
           break;
         }
         if (lane == 0) {
-          umma::mbar_arrive_expect_tx(&B->full[st], kStageBytes);
-          uint8_t* sa = smem + st * kStageBytes;
-          umma::bulk_g2s(sa, A + (int64_t)kb * (kSlices * kMTile * kBK), kABytes, &B->full[st]);
-          umma::bulk_g2s(sa + kABytes, Bm + (int64_t)kb * (kSlices * kNTile * kBK), kBBytes,
-                         &B->full[st]);
+          if (u < v.nkb) {
+            // the whole stage lands here: the A shares of the group and own B
+            umma::mbar_arrive_expect_tx(&B->full[st], kStageBytes);
+            uint8_t* sa = smem + st * kStageBytes;
+            const uint8_t* ga = A + (int64_t)u * kABytes;
+            if (v.nparts > 1)
+              umma::bulk_g2s_multicast(sa + a_lo, ga + a_lo, a_hi - a_lo, &B->full[st], v.mask);
+            else
+              umma::bulk_g2s(sa, ga, kABytes, &B->full[st]);
+            umma::bulk_g2s(sa + kABytes, Bm + (int64_t)u * kBBytes, kBBytes, &B->full[st]);
+          } else {
+            umma::mbar_arrive(&B->full[st]);  // no tile (or a shorter one): empty use
+          }
         }
         __syncwarp();
-        ++g;
       }
       if (!ok) break;
     }
-    // copies still in flight land before the CTA leaves
+    // Every stage use filled here has been released by all CTAs of the
+    // cluster: the copies this CTA multicast have landed and the MMA commits
+    // aimed at this CTA have arrived.
     for (uint32_t x = g > (uint32_t)kStages ? g - kStages : 0; x < g; ++x)
-      warp_wait(&B->full[x % kStages], (x / kStages) & 1);
+      warp_wait(&B->empty[x % kStages], (x / kStages) & 1);
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issue
     uint32_t g = 0;
     int li = 0;
-    for (int ii = beg; ii < end; ++ii, ++li) {
+    for (int sl = beg; sl < end; ++sl) {
       if (warp_failed(B)) break;
-      const OzItem it = sched.items[ii];
+      const SlotView v = slot_view(sched.items, sl, rank);
       // the epilogue has drained the previous tile's accumulators
-      if (li >= 1 && !warp_wait(&B->tempty, (li - 1) & 1)) {
+      if (v.nkb > 0 && li >= 1 && !warp_wait(&B->tempty, (li - 1) & 1)) {
         if (lane == 0) set_fail(B, ERR_TEMPTY);
         break;
       }
       umma::fence_after_sync();
-      const uint32_t d0 = tmem;
-      const int nkb = (it.k1 - it.k0) / kBK;
       bool ok = true;
-      for (int kb = 0; kb < nkb; ++kb, ++g) {
+      for (int u = 0; u < v.uses; ++u, ++g) {
         const int st = (int)(g % kStages);
         if (!warp_wait(&B->full[st], (g / kStages) & 1)) {
           if (lane == 0) set_fail(B, ERR_FULL);
@@ -274,15 +341,20 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         umma::fence_after_sync();
         if (lane == 0) {
-          const uint32_t a0 = umma::smem_u32(smem + st * kStageBytes);
-          issue_block(d0, a0, a0 + kABytes, kb > 0);
-          umma::mma_commit(&B->empty[st]);
+          if (u < v.nkb) {
+            const uint32_t a0 = umma::smem_u32(smem + st * kStageBytes);
+            issue_block(tmem, a0, a0 + kABytes, u > 0);
+          }
+          umma::mma_commit_multicast(&B->empty[st], kClusterMask);
         }
         __syncwarp();
       }
       if (!ok) break;
-      if (lane == 0) umma::mma_commit(&B->tfull);
-      __syncwarp();
+      if (v.nkb > 0) {
+        if (lane == 0) umma::mma_commit(&B->tfull);
+        __syncwarp();
+        ++li;
+      }
     }
     // every MMA issued above has completed before TMEM is released
     if (lane == 0) umma::mma_commit(&B->done);
@@ -297,9 +369,11 @@ __global__ void __launch_bounds__(kThreads, 1)
     double* red = reinterpret_cast<double*>(smem + kStages * kStageBytes) + (warp - 2) * 32 * kEpiStride;
     const int nq = gga ? 4 : 1;
     int li = 0;
-    for (int ii = beg; ii < end; ++ii, ++li) {
+    for (int sl = beg; sl < end; ++sl) {
       if (warp_failed(B)) break;
-      const OzItem it = sched.items[ii];
+      const OzItem it = sched.items[(int64_t)sl * kCluster + rank];
+      if (it.pb < 0) continue;
+      const int lc = li++;
       // Tile prologue, before the accumulators are ready: metadata, scales
       // and global indices.
       const int b = it.pb;
@@ -320,7 +394,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         gn_l = bfl[jl];
         ecz = exp_of_pow2(base[o.cz]);
       }
-      if (!warp_wait(&B->tfull, li & 1)) {
+      if (!warp_wait(&B->tfull, lc & 1)) {
         if (lane == 0) set_fail(B, ERR_TFULL);
         break;
       }
@@ -397,71 +471,113 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (tid == 0 && B->fail) atomicExch(err, B->fail);
   umma::fence_after_sync();
   if (warp == 0) umma::tmem_dealloc(tmem, kTmemCols);
+  // no CTA leaves while a peer of the cluster may still address its barriers
+  umma::cluster_sync();
+}
+
+template <int EPI>
+void set_smem_attr() {
+  static bool done = false;
+  if (!done) {
+    GB300_CUDA(cudaFuncSetAttribute(ozaki_kernel<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)ozaki_smem_bytes()));
+    done = true;
+  }
 }
 
 template <int EPI>
 void launch(const TasksDev& tk, const MixedPBDev& mp, const OzSchedule& sched, const double* f64,
             const __nv_bfloat16* dig, bool gga, double* out, int nbf, int* err, cudaStream_t s) {
-  if (sched.ncta <= 0) return;
-  const size_t smem = ozaki_smem_bytes();
-  static bool attr[2] = {false, false};
-  if (!attr[EPI]) {
-    GB300_CUDA(cudaFuncSetAttribute(ozaki_kernel<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem));
-    attr[EPI] = true;
-  }
-  ozaki_kernel<EPI><<<sched.ncta, kThreads, smem, s>>>(tk, mp, sched, f64, dig, gga ? 1 : 0, out,
-                                                       nbf, err);
-  GB300_CUDA(cudaGetLastError());
+  if (sched.nclusters <= 0) return;
+  set_smem_attr<EPI>();
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(sched.nclusters * kCluster);
+  cfg.blockDim = dim3(kThreads);
+  cfg.dynamicSmemBytes = ozaki_smem_bytes();
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = kCluster;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  GB300_CUDA(cudaLaunchKernelEx(&cfg, ozaki_kernel<EPI>, tk, mp, sched, f64, dig, gga ? 1 : 0, out,
+                                nbf, err));
 }
 
 }  // namespace
 
 size_t ozaki_smem_bytes() { return (size_t)kBarOffset + sizeof(Bars) + 1024; }
 
-int ozaki_schedule(std::vector<OzItem>& items, size_t begin, size_t end, int nsm,
-                   std::vector<int>& cta_off) {
-  const size_t n = end - begin;
+int ozaki_clusters() {
+  static int n = 0;
   if (n == 0) {
-    cta_off.push_back((int)begin);
+    set_smem_attr<EPI_X>();
+    set_smem_attr<EPI_V>();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(kCluster);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = ozaki_smem_bytes();
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = kCluster;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int nx = 0, nv = 0;
+    GB300_CUDA(cudaOccupancyMaxActiveClusters(&nx, ozaki_kernel<EPI_X>, &cfg));
+    GB300_CUDA(cudaOccupancyMaxActiveClusters(&nv, ozaki_kernel<EPI_V>, &cfg));
+    n = std::min(nx, nv);
+    if (n <= 0) throw std::runtime_error("tensor-core GEMM: no cluster of 4 CTAs fits the device");
+  }
+  return n;
+}
+
+int ozaki_schedule(const std::vector<OzItem>& items, size_t begin, size_t end, int nclusters,
+                   std::vector<OzItem>& slots, std::vector<int>& slot_off) {
+  // Slots: kCluster tiles taken in list order (the list holds tiles with the
+  // same A operand next to each other, so most slots hold one or two sharing
+  // groups); the last slot is padded with empty entries (pb = -1).
+  std::vector<OzItem> v;
+  for (size_t i = begin; i < end; ++i) v.push_back(items[i]);
+  const size_t nslot = (v.size() + kCluster - 1) / kCluster;
+  while (v.size() < nslot * kCluster) v.push_back(OzItem{-1, 0, 0, 0, 0});
+  const int ncl = (int)std::min<size_t>((size_t)std::max(nclusters, 1), nslot);
+  if (ncl == 0) {
+    slot_off.push_back((int)(slots.size() / kCluster));
     return 0;
   }
-  // Gangs of kGang CTAs take slots of kGang consecutive tiles (the list holds
-  // the tiles of one operand row next to each other, so a slot's tiles share
-  // their A operand); member j of the gang gets tile j of each of its slots.
-  // The members start together and run tiles of equal K, so they stream the
-  // same A blocks at about the same time and all but the first read hit L2.
-  // Slots go, in list order (point blocks in atom order), to the least loaded
-  // gang.
-  constexpr int kGang = 4;
-  const int ncta = (int)std::min<size_t>((size_t)std::max(nsm, 1), n);
-  const int g = ncta >= kGang ? kGang : 1;
-  const int ngang = ncta / g;  // every CTA gets at least one tile (n >= ncta)
-  auto cost = [](const OzItem& q) { return (q.k1 - q.k0) / kBK + 2; };
-  const std::vector<OzItem> v(items.begin() + begin, items.begin() + end);
+  // A slot costs its longest tile (all CTAs of a cluster step through the
+  // same stage uses) plus the epilogue; slots go, in list order (point blocks
+  // in atom order), to the least loaded cluster.
+  auto cost = [&](size_t s) {
+    int kb = 0;
+    for (int r = 0; r < kCluster; ++r) {
+      const OzItem& q = v[s * kCluster + r];
+      if (q.pb >= 0) kb = std::max(kb, (q.k1 - q.k0) / kBK);
+    }
+    return (long long)kb + 2;
+  };
   using Load = std::pair<long long, int>;
   std::priority_queue<Load, std::vector<Load>, std::greater<Load>> heap;
-  for (int c = 0; c < ngang; ++c) heap.push({0LL, c});
-  const int nused = ngang * g;
-  std::vector<std::vector<OzItem>> lists(nused);
-  for (size_t s0 = 0; s0 < v.size(); s0 += g) {
+  for (int c = 0; c < ncl; ++c) heap.push({0LL, c});
+  std::vector<std::vector<size_t>> lists(ncl);
+  for (size_t s = 0; s < nslot; ++s) {
     Load l = heap.top();
     heap.pop();
-    long long c = 0;
-    for (int k = 0; k < g && s0 + k < v.size(); ++k) {
-      lists[l.second * g + k].push_back(v[s0 + k]);
-      c = std::max<long long>(c, cost(v[s0 + k]));
-    }
-    l.first += c;
+    lists[l.second].push_back(s);
+    l.first += cost(s);
     heap.push(l);
   }
-  size_t at = begin;
-  for (int c = 0; c < nused; ++c) {
-    cta_off.push_back((int)at);
-    for (const OzItem& q : lists[c]) items[at++] = q;
+  for (int c = 0; c < ncl; ++c) {
+    slot_off.push_back((int)(slots.size() / kCluster));
+    for (size_t s : lists[c])
+      for (int r = 0; r < kCluster; ++r) slots.push_back(v[s * kCluster + r]);
   }
-  cta_off.push_back((int)at);
-  return nused;
+  slot_off.push_back((int)(slots.size() / kCluster));
+  return ncl;
 }
 
 // Self-test of the symmetric VXC GEMM: S = F Z^T + Z F^T (n x n) over k
@@ -520,8 +636,9 @@ double ozaki_selftest(int n, int k) {
   for (int m0 = 0; m0 < d.nu128; m0 += kMTile)
     for (int n0 = 0; n0 < d.nun; n0 += kNTile)
       if (m0 < n0 + kNTile) items.push_back(OzItem{0, m0, n0, 0, k2});
-  std::vector<int> cta_off;
-  const int ncta = ozaki_schedule(items, 0, items.size(), 148, cta_off);
+  std::vector<OzItem> slots;
+  std::vector<int> slot_off;
+  const int ncl = ozaki_schedule(items, 0, items.size(), ozaki_clusters(), slots, slot_off);
   int zero_i = 0;
   int64_t zero_l = 0;
   __nv_bfloat16* ddig;
@@ -536,10 +653,10 @@ double ozaki_selftest(int n, int k) {
   GB300_CUDA(cudaMalloc(&dnp, 4));
   GB300_CUDA(cudaMalloc(&dnu, 4));
   GB300_CUDA(cudaMalloc(&derr, 4));
-  GB300_CUDA(cudaMalloc(&doffs, cta_off.size() * 4));
+  GB300_CUDA(cudaMalloc(&doffs, slot_off.size() * 4));
   GB300_CUDA(cudaMalloc(&doff, 8));
   GB300_CUDA(cudaMalloc(&dz, 8));
-  GB300_CUDA(cudaMalloc(&ditems, items.size() * sizeof(OzItem)));
+  GB300_CUDA(cudaMalloc(&ditems, slots.size() * sizeof(OzItem)));
   GB300_CUDA(cudaMemcpy(ddig, dig.data(), dig.size() * 2, cudaMemcpyHostToDevice));
   GB300_CUDA(cudaMemcpy(df64, f64.data(), f64.size() * 8, cudaMemcpyHostToDevice));
   GB300_CUDA(cudaMemset(dA, 0, (size_t)n * n * 8));
@@ -547,10 +664,10 @@ double ozaki_selftest(int n, int k) {
   GB300_CUDA(cudaMemcpy(dnp, &np, 4, cudaMemcpyHostToDevice));
   GB300_CUDA(cudaMemcpy(dnu, &n, 4, cudaMemcpyHostToDevice));
   GB300_CUDA(cudaMemcpy(derr, &zero_i, 4, cudaMemcpyHostToDevice));
-  GB300_CUDA(cudaMemcpy(doffs, cta_off.data(), cta_off.size() * 4, cudaMemcpyHostToDevice));
+  GB300_CUDA(cudaMemcpy(doffs, slot_off.data(), slot_off.size() * 4, cudaMemcpyHostToDevice));
   GB300_CUDA(cudaMemcpy(doff, &zero_l, 8, cudaMemcpyHostToDevice));
   GB300_CUDA(cudaMemcpy(dz, &zero_l, 8, cudaMemcpyHostToDevice));
-  GB300_CUDA(cudaMemcpy(ditems, items.data(), items.size() * sizeof(OzItem), cudaMemcpyHostToDevice));
+  GB300_CUDA(cudaMemcpy(ditems, slots.data(), slots.size() * sizeof(OzItem), cudaMemcpyHostToDevice));
   TasksDev tk{};
   tk.npts_pad = dnp;
   tk.nbe_pad = dnu;
@@ -559,7 +676,7 @@ double ozaki_selftest(int n, int k) {
   tk.bf_list = dbf;
   tk.pt_off = dz;
   MixedPBDev mp{doff, doff};
-  launch<EPI_V>(tk, mp, OzSchedule{ditems, doffs, ncta}, df64, ddig, false, dA, n, derr, 0);
+  launch<EPI_V>(tk, mp, OzSchedule{ditems, doffs, ncl}, df64, ddig, false, dA, n, derr, 0);
   GB300_CUDA(cudaDeviceSynchronize());
   std::vector<double> C((size_t)n * n);
   int herr = 0;

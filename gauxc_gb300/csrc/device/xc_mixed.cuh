@@ -100,12 +100,14 @@ struct OzItem {
   int pb, m0, n0, k0, k1;
 };
 
-// Work list of one persistent GEMM launch: CTA c processes
-// items[cta_off[c] .. cta_off[c + 1]) in order.
+// Work list of one persistent GEMM launch on clusters of kCluster CTAs:
+// cluster c processes slots slot_off[c] .. slot_off[c + 1] - 1 in order; CTA
+// r of the cluster takes items[kCluster * slot + r] (pb < 0: none).
+constexpr int kCluster = 4;
 struct OzSchedule {
   const OzItem* items;
-  const int* cta_off;
-  int ncta;
+  const int* slot_off;
+  int nclusters;
 };
 
 void launch_collocation_masked(const ShellsDev& sh, const TasksDev& tk, const PBMaskDev& mk,
@@ -139,11 +141,14 @@ void launch_ozaki_v(const TasksDev& tk, const MixedPBDev& mp, const OzSchedule& 
                     const double* f64, const __nv_bfloat16* dig, bool gga, double* A, int nbf,
                     int* err, cudaStream_t s);
 
-// Host: order items[begin, end) into per-CTA lists for a persistent launch on
-// up to `nsm` CTAs (gangs of CTAs take slots of consecutive tiles, see
-// ozaki_gemm.cu); appends ncta + 1 absolute offsets to cta_off and returns ncta.
-int ozaki_schedule(std::vector<OzItem>& items, size_t begin, size_t end, int nsm,
-                   std::vector<int>& cta_off);
+// Host: group items[begin, end) into slots of kCluster tiles (list order;
+// tiles sharing an A operand should be adjacent) and distribute the slots
+// over up to `nclusters` clusters.  Appends the slots to `slots` and ncl + 1
+// absolute slot offsets to slot_off; returns ncl, the clusters to launch.
+int ozaki_schedule(const std::vector<OzItem>& items, size_t begin, size_t end, int nclusters,
+                   std::vector<OzItem>& slots, std::vector<int>& slot_off);
+// Clusters of the GEMM kernels that can be resident at once on this device.
+int ozaki_clusters();
 
 size_t ozaki_smem_bytes();
 // Self-test of the symmetric VXC GEMM (n x n output, k points); worst error
