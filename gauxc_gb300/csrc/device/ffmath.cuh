@@ -33,50 +33,35 @@ __device__ __forceinline__ long long fixed42(double v, int es) {
   return (b >> 63) ? -q : q;
 }
 
-// BF16 bit pattern of d * 2^(-7 i) for an integer |d| <= 255, i <= 5, by
-// integer operations: d becomes an exact float through the 1.5 * 2^23 bias,
-// its top 16 bits are the exact BF16 (at most 8 significant bits), and 7 i is
-// taken off the exponent field (never below 1 for these ranges).
-__device__ __forceinline__ unsigned bf16_digit(int d, int i) {
-  const float f = __int_as_float(0x4B400000 + d) - 12582912.f;
-  const unsigned b = __float_as_uint(f) >> 16;
-  return d ? b - ((unsigned)(7 * i) << 7) : 0u;
+// Balanced base-128 digits of q (|q| < 2^(7 S)): q = sum_i d_i 128^(S-1-i),
+// d_0 in [-128, 128], the others in [-64, 63]; store(i, x) receives the exact
+// float x = d_i 2^(-7 i), whose top 16 bits are its BF16 pattern (at most 8
+// significant bits).  Adding 64 128^k (k = 0..S-2) turns digits 1..S-1 into
+// the plain 7-bit fields f_i = d_i + 64 of u = q + bias (field i at bit
+// 7 (S-1-i)), and digit 0 into the arithmetic rest u >> 7 (S-1): no carry
+// chain.  OR-ing a field into the bits of 1.5 2^23 gives the float
+// 1.5 2^23 + f exactly, and one FMA by 2^(-7 i) takes the offset
+// (1.5 2^23 + 64) 2^(-7 i) off exactly.
+template <int S, typename Store>
+__device__ __forceinline__ void digits_f32(long long q, Store&& store) {
+  static_assert(S >= 2 && S <= 6, "fields below bit 35");
+  constexpr long long kBias = 64LL * ((1LL << (7 * (S - 1))) - 1) / 127;
+  const long long u = q + kBias;
+  const unsigned lo = (unsigned)u, hi = (unsigned)((unsigned long long)u >> 32);
+  const int d0 = (int)(u >> (7 * (S - 1)));
+  store(0, __int_as_float(0x4B400000 + d0) - 12582912.f);
+#pragma unroll
+  for (int i = 1; i < S; ++i) {
+    const int sh = 7 * (S - 1 - i);
+    const unsigned f = (sh + 7 <= 32 ? lo >> sh : __funnelshift_r(lo, hi, sh)) & 127u;
+    const float sc = __int_as_float((127 - 7 * i) << 23);
+    store(i, fmaf(__int_as_float(0x4B400000 | (int)f), sc, -12582976.f * sc));
+  }
 }
 
-// Balanced base-128 digits of q (|q| <= 2^42) as BF16 bit patterns of
-// d_i * 2^(-7 i), d_0 in [-128, 128], the others in [-64, 63].
-template <int S, typename Store>
-__device__ __forceinline__ void digits_bf16(long long q, Store&& store) {
-  int d[S];
-#pragma unroll
-  for (int i = S - 1; i > 0; --i) {
-    const int di = (int)((q + 64) & 127) - 64;
-    d[i] = di;
-    q = (q - di) >> 7;
-  }
-  d[0] = (int)q;
-#pragma unroll
-  for (int i = 0; i < S; ++i) store(i, bf16_digit(d[i], i));
-}
-
-// Balanced base-128 digits of q (|q| <= 2^42): q = sum_i d_i 128^(S-1-i),
-// d_0 in [-128, 128], others in [-64, 63].  Writes d_i * 2^(-7 i) (exact in bf16).
-template <int S, typename Store>
-__device__ __forceinline__ void digits(long long q, Store&& store) {
-  float d[S];
-#pragma unroll
-  for (int i = S - 1; i > 0; --i) {
-    const int di = (int)((q + 64) & 127) - 64;
-    d[i] = (float)di;
-    q = (q - di) >> 7;
-  }
-  d[0] = (float)(int)q;
-  float sc = 1.f;
-#pragma unroll
-  for (int i = 0; i < S; ++i) {
-    store(i, d[i] * sc);
-    sc *= (1.f / 128.f);
-  }
+// Two BF16 patterns in one word: the top halves of floats a (low) and b (high).
+__device__ __forceinline__ unsigned pack_bf16x2(float a, float b) {
+  return __byte_perm(__float_as_uint(a), __float_as_uint(b), 0x7632);
 }
 
 // v = hi + lo with hi the leading 24 bits of v (truncated) and lo the rest

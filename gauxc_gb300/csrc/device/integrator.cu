@@ -543,19 +543,35 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
     cur.max_nu_pad = std::max(cur.max_nu_pad, nu_pad[i]);
     for (int b = 0; b < (npts_pad[i] + 127) / 128; ++b) coll.push_back(make_int2(i, b));
     const PBDims d(npts_pad[i], nu[i]);
-    // tiles of one A row block and K chunk next to each other (they share
-    // A); the full-length K chunks first, so that a cluster slot rarely
-    // mixes tiles of different K
-    const int nfull = d.nu16 / kMaxK, nchunk = (d.nu16 + kMaxK - 1) / kMaxK;
-    for (int pass = 0; pass < 2; ++pass)
+    // Density tiles in cluster-slot order: the (m0, n0) tiles ("chains") in
+    // row-major order, four per block (the last block of a point block
+    // padded with empty entries); a block runs its chains' K chunks in
+    // consecutive slots, so each CTA sums a tile's chunks before the phi
+    // contraction and the chains of one row block share their A blocks.
+    {
+      const int nchunk = (d.nu16 + kMaxK - 1) / kMaxK;
+      std::vector<std::pair<int, int>> ch;
       for (int m0 = 0; m0 < d.nu128; m0 += kMTile)
-        for (int c = pass ? nfull : 0; c < (pass ? nchunk : nfull); ++c)
-          for (int n0 = 0; n0 < d.np; n0 += kNTile)
-            xi.push_back(OzItem{i, m0, n0, c * kMaxK, std::min((c + 1) * kMaxK, d.nu16)});
+        for (int n0 = 0; n0 < d.np; n0 += kNTile) ch.push_back({m0, n0});
+      for (size_t c0 = 0; c0 < ch.size(); c0 += kCluster)
+        for (int c = 0; c < nchunk; ++c)
+          for (int r = 0; r < kCluster; ++r) {
+            if (c0 + r >= ch.size()) {
+              xi.push_back(OzItem{-1, 0, 0, 0, 0, 0, 0});
+              continue;
+            }
+            xi.push_back(OzItem{i, ch[c0 + r].first, ch[c0 + r].second, c * kMaxK,
+                                std::min((c + 1) * kMaxK, d.nu16), 0, 0});
+            oz_set_operands(xi.back(), d, dig_off[i], false);
+          }
+    }
     // symmetric VXC: tiles reaching the upper triangle, K = phi | Z
     for (int m0 = 0; m0 < d.nu128; m0 += kMTile)
       for (int n0 = 0; n0 < d.nun; n0 += kNTile)
-        if (m0 < n0 + kNTile) vi.push_back(OzItem{i, m0, n0, 0, 2 * d.np});
+        if (m0 < n0 + kNTile) {
+          vi.push_back(OzItem{i, m0, n0, 0, 2 * d.np, 0, 0});
+          oz_set_operands(vi.back(), d, dig_off[i], true);
+        }
   }
   if (npb > 0) close_batch(npb);
   {
@@ -563,7 +579,8 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
     for (int lev = 2; lev <= kLevels; ++lev)
       for (int i = 1; i <= kSlices; ++i)
         if (lev - i >= 1 && lev - i <= kSlices) ++npairs;
-    for (const OzItem& q : xi) stats.tensor_flops_x += 2.0 * kMTile * kNTile * (q.k1 - q.k0) * npairs;
+    for (const OzItem& q : xi)
+      if (q.pb >= 0) stats.tensor_flops_x += 2.0 * kMTile * kNTile * (q.k1 - q.k0) * npairs;
     for (const OzItem& q : vi) stats.tensor_flops_v += 2.0 * kMTile * kNTile * (q.k1 - q.k0) * npairs;
   }
   // per-cluster slot lists of every persistent GEMM launch

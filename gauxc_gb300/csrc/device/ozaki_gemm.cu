@@ -163,18 +163,31 @@ __device__ __forceinline__ void reduce16(float (&h)[16], float (&l)[16], int lan
 }
 
 // This thread's lane of TMEM columns [col, col + 16) of the six levels, summed
-// into float-float values.
+// in level order into float-float values (three levels per TMEM load) and
+// added to hi + lo when `acc` (the earlier K chunks of the tile).
 __device__ __forceinline__ void drain_levels(uint32_t tb, uint32_t col, float (&hi)[16],
-                                             float (&lo)[16]) {
-  const uint32_t t[6] = {tb + col, tb + kNTile + col, tb + 2 * kNTile + col,
-                         tb + 3 * kNTile + col, tb + 4 * kNTile + col, tb + 5 * kNTile + col};
-  float v[6][16];
-  umma::tmem_ld16x6(t, v);
+                                             float (&lo)[16], bool acc) {
+  float v[3][16];
+  umma::tmem_ld16x3(tb + col, tb + kNTile + col, tb + 2 * kNTile + col, v);
 #pragma unroll
   for (int n = 0; n < 16; ++n) {
-    float s = v[0][n], e = 0.f;
+    float s = acc ? hi[n] : 0.f, e = acc ? lo[n] : 0.f;
 #pragma unroll
-    for (int a = 1; a < 6; ++a) {
+    for (int a = 0; a < 3; ++a) {
+      float u, d;
+      ff::two_sum(s, v[a][n], u, d);
+      s = u;
+      e += d;
+    }
+    hi[n] = s;
+    lo[n] = e;
+  }
+  umma::tmem_ld16x3(tb + 3 * kNTile + col, tb + 4 * kNTile + col, tb + 5 * kNTile + col, v);
+#pragma unroll
+  for (int n = 0; n < 16; ++n) {
+    float s = hi[n], e = lo[n];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
       float u, d;
       ff::two_sum(s, v[a][n], u, d);
       s = u;
@@ -195,46 +208,36 @@ struct SlotView {
   uint16_t mask;
 };
 
+struct SlotItems {
+  OzItem q[kCluster];
+};
+
+__device__ __forceinline__ void load_slot(const OzItem* items, int slot, SlotItems& s) {
+#pragma unroll
+  for (int r = 0; r < kCluster; ++r) s.q[r] = items[(int64_t)slot * kCluster + r];
+}
+
 __device__ __forceinline__ bool same_a(const OzItem& a, const OzItem& b) {
   return a.pb == b.pb && a.m0 == b.m0 && a.k0 == b.k0 && a.k1 == b.k1;
 }
 
-__device__ __forceinline__ SlotView slot_view(const OzItem* items, int slot, int rank) {
-  OzItem q[kCluster];
+__device__ __forceinline__ SlotView view_of(const SlotItems& s, int rank) {
   SlotView v;
 #pragma unroll
-  for (int r = 0; r < kCluster; ++r) {
-    q[r] = items[(int64_t)slot * kCluster + r];
-    if (r == rank) v.it = q[r];
-  }
+  for (int r = 0; r < kCluster; ++r)
+    if (r == rank) v.it = s.q[r];
   v.nkb = v.it.pb >= 0 ? (v.it.k1 - v.it.k0) / kBK : 0;
   v.uses = 0;
   v.mask = 0;
 #pragma unroll
   for (int r = 0; r < kCluster; ++r) {
-    if (q[r].pb < 0) continue;
-    v.uses = max(v.uses, (q[r].k1 - q[r].k0) / kBK);
-    if (v.it.pb >= 0 && same_a(q[r], v.it)) v.mask |= (uint16_t)(1u << r);
+    if (s.q[r].pb < 0) continue;
+    v.uses = max(v.uses, (s.q[r].k1 - s.q[r].k0) / kBK);
+    if (v.it.pb >= 0 && same_a(s.q[r], v.it)) v.mask |= (uint16_t)(1u << r);
   }
   v.part = __popc(v.mask & ((1u << rank) - 1));
   v.nparts = __popc(v.mask);
   return v;
-}
-
-// First element of the tile row block holding rows [m0, m0 + TR) of an
-// operand, for EPI's A (M) and B (N) operands.
-template <int EPI>
-__device__ __forceinline__ void operands(const OzItem& it, const TasksDev& tk,
-                                         const MixedPBDev& mp, const __nv_bfloat16* dig,
-                                         const __nv_bfloat16*& A, const __nv_bfloat16*& B) {
-  const int b = it.pb;
-  const PBDims d(tk.npts_pad[b], tk.nbe[b]);
-  const __nv_bfloat16* base = dig + mp.dig_off[b];
-  const int64_t nkb = (EPI == EPI_X ? d.nu16 : 2 * d.np) / kBK;
-  A = base + (EPI == EPI_X ? d.pd() : d.va()) +
-      (int64_t)(it.m0 / kMTile) * nkb * (kSlices * kMTile * kBK);
-  B = base + (EPI == EPI_X ? d.fd() : d.vb()) +
-      (int64_t)(it.n0 / kNTile) * nkb * (kSlices * kNTile * kBK);
 }
 
 template <int EPI>
@@ -273,16 +276,16 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (warp == 0) {
     // ------------------------------------------------------------ producer
     uint32_t g = 0;
+    SlotItems cur, nxt;
+    if (beg < end) load_slot(sched.items, beg, cur);
+    nxt = cur;
     for (int sl = beg; sl < end; ++sl) {
       if (warp_failed(B)) break;
-      const SlotView v = slot_view(sched.items, sl, rank);
-      const uint8_t *A = nullptr, *Bm = nullptr;
-      if (v.nkb > 0) {
-        const __nv_bfloat16 *a, *b;
-        operands<EPI>(v.it, tk, mp, dig, a, b);
-        A = reinterpret_cast<const uint8_t*>(a) + (int64_t)(v.it.k0 / kBK) * kABytes;
-        Bm = reinterpret_cast<const uint8_t*>(b) + (int64_t)(v.it.k0 / kBK) * kBBytes;
-      }
+      // the next slot's entries load while this slot's copies are issued
+      if (sl + 1 < end) load_slot(sched.items, sl + 1, nxt);
+      const SlotView v = view_of(cur, rank);
+      const uint8_t* A = reinterpret_cast<const uint8_t*>(dig + v.it.a);
+      const uint8_t* Bm = reinterpret_cast<const uint8_t*>(dig + v.it.b);
       const uint32_t a_lo = (uint32_t)(v.part * kABytes / max(v.nparts, 1));
       const uint32_t a_hi = (uint32_t)((v.part + 1) * kABytes / max(v.nparts, 1));
       bool ok = true;
@@ -312,6 +315,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         __syncwarp();
       }
       if (!ok) break;
+      cur = nxt;
     }
     // Every stage use filled here has been released by all CTAs of the
     // cluster: the copies this CTA multicast have landed and the MMA commits
@@ -322,9 +326,13 @@ __global__ void __launch_bounds__(kThreads, 1)
     // ------------------------------------------------------------ MMA issue
     uint32_t g = 0;
     int li = 0;
+    SlotItems cur, nxt;
+    if (beg < end) load_slot(sched.items, beg, cur);
+    nxt = cur;
     for (int sl = beg; sl < end; ++sl) {
       if (warp_failed(B)) break;
-      const SlotView v = slot_view(sched.items, sl, rank);
+      if (sl + 1 < end) load_slot(sched.items, sl + 1, nxt);
+      const SlotView v = view_of(cur, rank);
       // the epilogue has drained the previous tile's accumulators
       if (v.nkb > 0 && li >= 1 && !warp_wait(&B->tempty, (li - 1) & 1)) {
         if (lane == 0) set_fail(B, ERR_TEMPTY);
@@ -355,6 +363,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         __syncwarp();
         ++li;
       }
+      cur = nxt;
     }
     // every MMA issued above has completed before TMEM is released
     if (lane == 0) umma::mma_commit(&B->done);
@@ -369,11 +378,20 @@ __global__ void __launch_bounds__(kThreads, 1)
     double* red = reinterpret_cast<double*>(smem + kStages * kStageBytes) + (warp - 2) * 32 * kEpiStride;
     const int nq = gga ? 4 : 1;
     int li = 0;
+    // D of the tile in hand (float-float), summed over its K chunks when the
+    // next entry continues the same tile (density)
+    float hi[2][16], lo[2][16];
+    bool acc = false;
+    OzItem nit = beg < end ? sched.items[(int64_t)beg * kCluster + rank] : OzItem{};
     for (int sl = beg; sl < end; ++sl) {
       if (warp_failed(B)) break;
-      const OzItem it = sched.items[(int64_t)sl * kCluster + rank];
+      const OzItem it = nit;
+      // the next tile's entry loads while this one is processed
+      if (sl + 1 < end) nit = sched.items[(int64_t)(sl + 1) * kCluster + rank];
       if (it.pb < 0) continue;
       const int lc = li++;
+      const bool last = EPI == EPI_V || sl + 1 == end || nit.pb != it.pb || nit.m0 != it.m0 ||
+                        nit.n0 != it.n0 || nit.k0 != it.k1;
       // Tile prologue, before the accumulators are ready: metadata, scales
       // and global indices.
       const int b = it.pb;
@@ -383,11 +401,14 @@ __global__ void __launch_bounds__(kThreads, 1)
       const int i = it.m0 + row;               // tile row (basis function nu / mu)
       const int jl = it.n0 + c0 * 16 + lane;   // this lane's column of the warp's 32
       int e_row = 0, e_col = 0, gm_l = 0, gn_l = 0, ecz = 0;
+      int64_t gpt = 0;
       const float2* phi2 = nullptr;
+      float2 pf[16];  // phi[nu = i][p] of the pass in hand, float-float
       if (EPI == EPI_X) {
         e_row = exp_of_pow2(base[o.r + i]);
         e_col = exp_of_pow2(base[o.sp + jl]);
-        phi2 = reinterpret_cast<const float2*>(base + o.phi2);
+        gpt = tk.pt_off[b] + it.n0;
+        phi2 = reinterpret_cast<const float2*>(base + o.phi2) + i;
       } else {
         const int* bfl = tk.bf_list + tk.bf_off[b];
         gm_l = bfl[i];
@@ -400,17 +421,38 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       umma::fence_after_sync();
       // levels -> float-float in registers, then TMEM goes back to the MMAs
-      float hi[2][16], lo[2][16];
-      drain_levels(lane_base, c0 * 16, hi[0], lo[0]);
-      drain_levels(lane_base, c0 * 16 + 16, hi[1], lo[1]);
+      drain_levels(lane_base, c0 * 16, hi[0], lo[0], acc);
+      drain_levels(lane_base, c0 * 16 + 16, hi[1], lo[1], acc);
       umma::fence_before_sync();
       __syncwarp();
       if (lane == 0) umma::mbar_arrive(&B->tempty);
+      acc = !last;
+      if (!last) continue;
       if (EPI == EPI_X) {
+        const float2* f = phi2 + (int64_t)(it.n0 + c0 * 16) * d.nu128;
+#pragma unroll
+        for (int n = 0; n < 16; ++n) pf[n] = f[(int64_t)n * d.nu128];
+        // the second column chunk waits in shared memory (registers)
+        float* park = reinterpret_cast<float*>(red);
+#pragma unroll
+        for (int n = 0; n < 16; ++n) {
+          park[n * 32 + lane] = hi[1][n];
+          park[(16 + n) * 32 + lane] = lo[1][n];
+        }
+      }
+      if (EPI == EPI_X) {
+        // passes (k, q): column chunk c0 + k, value q (phi, then 2 grad phi)
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
           const int c = c0 + k;
-          const int64_t g0 = tk.pt_off[b] + it.n0 + c * 16;
+          if (k == 1) {
+            const float* park = reinterpret_cast<const float*>(red);
+#pragma unroll
+            for (int n = 0; n < 16; ++n) {
+              hi[1][n] = park[n * 32 + lane];
+              lo[1][n] = park[(16 + n) * 32 + lane];
+            }
+          }
           // X'[nu, p] = 2^(er + esp - 13) D, a power of two times D
 #pragma unroll
           for (int n = 0; n < 16; ++n) {
@@ -420,20 +462,26 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
           for (int q = 0; q < nq; ++q) {
             float h[16], l[16];
-            const float2* f = phi2 + q * o.blk + (int64_t)(it.n0 + c * 16) * d.nu128 + i;
 #pragma unroll
             for (int n = 0; n < 16; ++n) {
-              float2 fv = f[(int64_t)n * d.nu128];
+              float2 fv = pf[n];
               if (q) fv = make_float2(2.f * fv.x, 2.f * fv.y);
               const float2 t = ff::mul(make_float2(hi[k][n], lo[k][n]), fv);
               h[n] = t.x;
               l[n] = t.y;
             }
+            // the next pass's phi values load while this pass is reduced
+            if (q + 1 < nq || k == 0) {
+              const int qn = q + 1 < nq ? q + 1 : 0, cn = q + 1 < nq ? c : c + 1;
+              const float2* f = phi2 + qn * o.blk + (int64_t)(it.n0 + cn * 16) * d.nu128;
+#pragma unroll
+              for (int n = 0; n < 16; ++n) pf[n] = f[(int64_t)n * d.nu128];
+            }
             reduce16(h, l, lane);
             if ((lane & 1) == 0) {
               const int n = ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 +
                             ((lane >> 1) & 1);
-              atomicAdd(&out[4 * (g0 + n) + q], ff::to_double_fast(h[0], l[0], 0));
+              atomicAdd(&out[4 * (gpt + c * 16 + n) + q], ff::to_double_fast(h[0], l[0], 0));
             }
           }
         }
@@ -537,21 +585,20 @@ int ozaki_clusters() {
 
 int ozaki_schedule(const std::vector<OzItem>& items, size_t begin, size_t end, int nclusters,
                    std::vector<OzItem>& slots, std::vector<int>& slot_off) {
-  // Slots: kCluster tiles taken in list order (the list holds tiles with the
-  // same A operand next to each other, so most slots hold one or two sharing
-  // groups); the last slot is padded with empty entries (pb = -1).
+  // Slots: kCluster entries taken in list order; the last slot is padded
+  // with empty entries (pb = -1).
   std::vector<OzItem> v;
   for (size_t i = begin; i < end; ++i) v.push_back(items[i]);
   const size_t nslot = (v.size() + kCluster - 1) / kCluster;
-  while (v.size() < nslot * kCluster) v.push_back(OzItem{-1, 0, 0, 0, 0});
-  const int ncl = (int)std::min<size_t>((size_t)std::max(nclusters, 1), nslot);
-  if (ncl == 0) {
-    slot_off.push_back((int)(slots.size() / kCluster));
-    return 0;
-  }
+  while (v.size() < nslot * kCluster) v.push_back(OzItem{-1, 0, 0, 0, 0, 0, 0});
+  // Units: runs of slots in which every CTA continues the K range of the
+  // same tile (the K chunks of a chain) stay together on one cluster.
+  auto continues = [](const OzItem& a, const OzItem& b) {
+    if (a.pb < 0 || b.pb < 0) return a.pb < 0 && b.pb < 0;
+    return a.pb == b.pb && a.m0 == b.m0 && a.n0 == b.n0 && b.k0 == a.k1;
+  };
   // A slot costs its longest tile (all CTAs of a cluster step through the
-  // same stage uses) plus the epilogue; slots go, in list order (point blocks
-  // in atom order), to the least loaded cluster.
+  // same stage uses) plus the epilogue.
   auto cost = [&](size_t s) {
     int kb = 0;
     for (int r = 0; r < kCluster; ++r) {
@@ -560,15 +607,33 @@ int ozaki_schedule(const std::vector<OzItem>& items, size_t begin, size_t end, i
     }
     return (long long)kb + 2;
   };
+  std::vector<size_t> ustart;
+  for (size_t s = 0; s < nslot; ++s) {
+    bool cont = s > 0;
+    for (int r = 0; r < kCluster && cont; ++r)
+      cont = continues(v[(s - 1) * kCluster + r], v[s * kCluster + r]);
+    if (!cont) ustart.push_back(s);
+  }
+  ustart.push_back(nslot);
+  const size_t nunit = ustart.size() - 1;
+  const int ncl = (int)std::min<size_t>((size_t)std::max(nclusters, 1), nunit);
+  if (ncl == 0) {
+    slot_off.push_back((int)(slots.size() / kCluster));
+    return 0;
+  }
+  // Units go, in list order (point blocks in atom order), to the least
+  // loaded cluster.
   using Load = std::pair<long long, int>;
   std::priority_queue<Load, std::vector<Load>, std::greater<Load>> heap;
   for (int c = 0; c < ncl; ++c) heap.push({0LL, c});
   std::vector<std::vector<size_t>> lists(ncl);
-  for (size_t s = 0; s < nslot; ++s) {
+  for (size_t u = 0; u < nunit; ++u) {
     Load l = heap.top();
     heap.pop();
-    lists[l.second].push_back(s);
-    l.first += cost(s);
+    for (size_t s = ustart[u]; s < ustart[u + 1]; ++s) {
+      lists[l.second].push_back(s);
+      l.first += cost(s);
+    }
     heap.push(l);
   }
   for (int c = 0; c < ncl; ++c) {
@@ -635,7 +700,10 @@ double ozaki_selftest(int n, int k) {
   std::vector<OzItem> items;
   for (int m0 = 0; m0 < d.nu128; m0 += kMTile)
     for (int n0 = 0; n0 < d.nun; n0 += kNTile)
-      if (m0 < n0 + kNTile) items.push_back(OzItem{0, m0, n0, 0, k2});
+      if (m0 < n0 + kNTile) {
+        items.push_back(OzItem{0, m0, n0, 0, k2, 0, 0});
+        oz_set_operands(items.back(), d, 0, true);
+      }
   std::vector<OzItem> slots;
   std::vector<int> slot_off;
   const int ncl = ozaki_schedule(items, 0, items.size(), ozaki_clusters(), slots, slot_off);

@@ -32,13 +32,12 @@ __device__ __forceinline__ void store_digits8(const T (&x)[8], const int (&es)[8
                                               __nv_bfloat16* out, int64_t plane) {
   uint32_t w[kSlices][4];
 #pragma unroll
-  for (int e = 0; e < 8; ++e)
-    ff::digits_bf16<kSlices>(ff::fixed42(x[e], es[e]), [&](int i, unsigned h) {
-      if (e & 1)
-        w[i][e >> 1] |= h << 16;
-      else
-        w[i][e >> 1] = h;
-    });
+  for (int e = 0; e < 8; e += 2) {
+    float a[kSlices];
+    ff::digits_f32<kSlices>(ff::fixed42(x[e], es[e]), [&](int i, float v) { a[i] = v; });
+    ff::digits_f32<kSlices>(ff::fixed42(x[e + 1], es[e + 1]),
+                            [&](int i, float v) { w[i][e >> 1] = ff::pack_bf16x2(a[i], v); });
+  }
 #pragma unroll
   for (int i = 0; i < kSlices; ++i)
     __stcs(reinterpret_cast<uint4*>(out + i * plane), make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]));

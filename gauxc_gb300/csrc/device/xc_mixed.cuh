@@ -95,10 +95,24 @@ struct MixedPBDev {
 };
 
 // One tensor-core GEMM tile: output rows [m0, m0+128) x cols [n0, n0+64),
-// K range [k0, k1) of point block pb.
+// K range [k0, k1) of point block pb; a / b: bf16 element offsets in the
+// digit work space of K block k0 of the tile's A row block and B row block
+// (oz_set_operands).
 struct OzItem {
   int pb, m0, n0, k0, k1;
+  int64_t a, b;
 };
+
+// Fills it.a / it.b for a density (vxc false) or VXC (vxc true) tile of a
+// point block with dimensions d whose digits start at element dig_off.
+inline void oz_set_operands(OzItem& it, const PBDims& d, int64_t dig_off, bool vxc) {
+  const int64_t nkb = (vxc ? 2 * d.np : d.nu16) / kBK;
+  const int64_t kb0 = it.k0 / kBK;
+  it.a = dig_off + (vxc ? d.va() : d.pd()) +
+         ((int64_t)(it.m0 / kMTile) * nkb + kb0) * (kSlices * kMTile * kBK);
+  it.b = dig_off + (vxc ? d.vb() : d.fd()) +
+         ((int64_t)(it.n0 / kNTile) * nkb + kb0) * (kSlices * kNTile * kBK);
+}
 
 // Work list of one persistent GEMM launch on clusters of kCluster CTAs:
 // cluster c processes slots slot_off[c] .. slot_off[c + 1] - 1 in order; CTA
