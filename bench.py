@@ -538,6 +538,10 @@ def main():
                  for k, v in kt.items()},
         setup_s=dict(load_balancer=ctx["t_lb"], ssf_weights=ctx["t_w"]),
         timed_wall_s=t_all)
+    if mixed:
+        for k, key in (("density", "tensor_flops_x"), ("vxc", "tensor_flops_v")):
+            if k in line["kernels"] and kt[k]["ms"] > 0:
+                line["kernels"][k]["tensor_tflops"] = stats[key] * args.steps / (kt[k]["ms"] * 1e-3) / 1e12
     print(json.dumps(line), flush=True)
     return 0
 

@@ -117,13 +117,14 @@ __device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity) {
 // in shared memory, so one operand of 64 (j1 - j0 + 1) rows) accumulates into
 // levels i + j0 .. i + j1 (TMEM columns 64 (i + j0) ..), all pairs with
 // i + j <= 5.  On a tile's first block the two plane-0 MMAs, which cover all
-// six levels, overwrite instead of accumulating.
-__device__ __forceinline__ void issue_block(uint32_t d0, uint32_t a0, uint32_t b0, bool acc_prev) {
+// six levels, overwrite instead of accumulating.  da / db: descriptors of
+// the stage's A and B tiles; a plane further on is a constant added to the
+// descriptor's address field (bytes / 16, no carry out of the field).
+__device__ __forceinline__ void issue_block(uint32_t d0, uint64_t da, uint64_t db, bool acc_prev) {
   auto mma = [&](int i, int j0, int nplanes, bool first) {
-    const uint64_t ad = umma::smem_desc(a0 + i * kAPlane, 128, (kBK / 8) * 128);
-    const uint64_t bd = umma::smem_desc(b0 + j0 * kBPlane, 128, (kBK / 8) * 128);
-    const uint32_t idesc = umma::idesc_bf16_f32(kMTile, kNTile * nplanes);
-    umma::mma_bf16(d0 + (i + j0) * kNTile, ad, bd, idesc, (acc_prev || !first) ? 1u : 0u);
+    umma::mma_bf16(d0 + (i + j0) * kNTile, da + (uint64_t)((i * kAPlane) >> 4),
+                   db + (uint64_t)((j0 * kBPlane) >> 4), umma::idesc_bf16_f32(kMTile, kNTile * nplanes),
+                   (acc_prev || !first) ? 1u : 0u);
   };
   mma(0, 0, 4, true);   // levels 0-3
   mma(0, 4, 2, true);   // levels 4-5
@@ -163,33 +164,25 @@ __device__ __forceinline__ void reduce16(float (&h)[16], float (&l)[16], int lan
 }
 
 // This thread's lane of TMEM columns [col, col + 16) of the six levels, summed
-// in level order into float-float values (three levels per TMEM load) and
-// added to hi + lo when `acc` (the earlier K chunks of the tile).
+// into float-float values and added to hi + lo when `acc` (the earlier K
+// chunks of the tile).  Levels 0-2 enter through exact two-sums; levels 3-5
+// (below 2^-21 of the products' magnitude) are first added in FP32, whose
+// rounding (2^-24 of level 3) stays under the error of the 42-bit digits.
 __device__ __forceinline__ void drain_levels(uint32_t tb, uint32_t col, float (&hi)[16],
                                              float (&lo)[16], bool acc) {
   float v[3][16];
+  umma::tmem_ld16x3(tb + 3 * kNTile + col, tb + 4 * kNTile + col, tb + 5 * kNTile + col, v);
+  float t[16];
+#pragma unroll
+  for (int n = 0; n < 16; ++n) t[n] = v[0][n] + (v[1][n] + v[2][n]);
   umma::tmem_ld16x3(tb + col, tb + kNTile + col, tb + 2 * kNTile + col, v);
 #pragma unroll
   for (int n = 0; n < 16; ++n) {
     float s = acc ? hi[n] : 0.f, e = acc ? lo[n] : 0.f;
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
+    for (int a = 0; a < 4; ++a) {
       float u, d;
-      ff::two_sum(s, v[a][n], u, d);
-      s = u;
-      e += d;
-    }
-    hi[n] = s;
-    lo[n] = e;
-  }
-  umma::tmem_ld16x3(tb + 3 * kNTile + col, tb + 4 * kNTile + col, tb + 5 * kNTile + col, v);
-#pragma unroll
-  for (int n = 0; n < 16; ++n) {
-    float s = hi[n], e = lo[n];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      float u, d;
-      ff::two_sum(s, v[a][n], u, d);
+      ff::two_sum(s, a < 3 ? v[a][n] : t[n], u, d);
       s = u;
       e += d;
     }
@@ -324,7 +317,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       warp_wait(&B->empty[x % kStages], (x / kStages) & 1);
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issue
-    uint32_t g = 0;
+    // descriptors of stage 0; stage st is st * kStageBytes / 16 further
+    const uint64_t da0 = umma::smem_desc(umma::smem_u32(smem), 128, (kBK / 8) * 128);
+    const uint64_t db0 = umma::smem_desc(umma::smem_u32(smem) + kABytes, 128, (kBK / 8) * 128);
+    uint32_t g = 0, st = 0, ph = 0;  // stage use, its stage and phase parity
     int li = 0;
     SlotItems cur, nxt;
     if (beg < end) load_slot(sched.items, beg, cur);
@@ -341,8 +337,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       umma::fence_after_sync();
       bool ok = true;
       for (int u = 0; u < v.uses; ++u, ++g) {
-        const int st = (int)(g % kStages);
-        if (!warp_wait(&B->full[st], (g / kStages) & 1)) {
+        if (!warp_wait(&B->full[st], ph)) {
           if (lane == 0) set_fail(B, ERR_FULL);
           ok = false;
           break;
@@ -350,12 +345,16 @@ __global__ void __launch_bounds__(kThreads, 1)
         umma::fence_after_sync();
         if (lane == 0) {
           if (u < v.nkb) {
-            const uint32_t a0 = umma::smem_u32(smem + st * kStageBytes);
-            issue_block(tmem, a0, a0 + kABytes, u > 0);
+            const uint64_t so = (uint64_t)((st * kStageBytes) >> 4);
+            issue_block(tmem, da0 + so, db0 + so, u > 0);
           }
           umma::mma_commit_multicast(&B->empty[st], kClusterMask);
         }
         __syncwarp();
+        if (++st == kStages) {
+          st = 0;
+          ph ^= 1;
+        }
       }
       if (!ok) break;
       if (v.nkb > 0) {
