@@ -63,7 +63,8 @@ namespace {
 
 constexpr int kStages = 5;
 constexpr int kEpiWarps = 8;  // two per TMEM lane quarter, 32 columns each
-constexpr int kThreads = 64 + 32 * kEpiWarps;
+constexpr int kHelpWarps = 2;  // process the chunks drained by the quarter-1 warps
+constexpr int kThreads = 64 + 32 * (kEpiWarps + kHelpWarps);
 constexpr int kAccs = kLevels - 1;  // exact level accumulators (i + j = 0..5)
 constexpr int kAPlane = kMTile * kBK * 2;  // bytes of one digit plane of an A tile (4 KB)
 constexpr int kBPlane = kNTile * kBK * 2;  // bytes of one digit plane of a B tile (2 KB)
@@ -71,9 +72,11 @@ constexpr int kABytes = kSlices * kAPlane;
 constexpr int kBBytes = kSlices * kBPlane;
 constexpr int kStageBytes = kABytes + kBBytes;
 constexpr uint32_t kTmemCols = 512;  // six levels x 64 columns (384) rounded up
-constexpr int kEpiStride = 17;  // padded row of a warp's 32 x 16 transposition tile
-constexpr int kEpiBytes = kEpiWarps * 32 * kEpiStride * 8;
-constexpr int kBarOffset = kStages * kStageBytes + kEpiBytes;
+constexpr int kChunkBytes = 32 * 16 * 8;  // one unit's data: 32 rows x 16 columns, 8 bytes each
+constexpr int kWorkWarps = kEpiWarps - 2;  // draining warps that also process (not quarter 1)
+constexpr int kRedOffset = kStages * kStageBytes;  // per working warp: parked chunk / transposition
+constexpr int kHandOffset = kRedOffset + kWorkWarps * kChunkBytes;
+constexpr int kBarOffset = kHandOffset + 4 * kChunkBytes;  // the four quarter-1 chunks
 constexpr uint32_t kWaitLimit = 1u << 22;
 constexpr uint16_t kClusterMask = (1u << kCluster) - 1;
 static_assert(kBK == 16, "one MMA (K = 16) per operand tile");
@@ -83,13 +86,15 @@ static_assert(kSlices == 6 && kLevels == 7, "MMA grouping below assumes 6 digits
 
 enum { EPI_X = 0, EPI_V = 1 };
 // error codes: which wait expired
-enum { ERR_EMPTY = 1, ERR_TEMPTY = 2, ERR_FULL = 3, ERR_TFULL = 4 };
+enum { ERR_EMPTY = 1, ERR_TEMPTY = 2, ERR_FULL = 3, ERR_TFULL = 4, ERR_HAND = 5 };
 
 struct Bars {
   uint64_t full[kStages];
   uint64_t empty[kStages];
   uint64_t tfull;
   uint64_t tempty;
+  uint64_t hfull;   // quarter-1 chunks handed over (2 arrivals)
+  uint64_t hempty;  // and processed (kHelpWarps arrivals)
   uint64_t done;
   uint32_t tmem_slot;
   int fail;
@@ -164,12 +169,12 @@ __device__ __forceinline__ void reduce16(float (&h)[16], float (&l)[16], int lan
 }
 
 // This thread's lane of TMEM columns [col, col + 16) of the six levels, summed
-// into float-float values and added to hi + lo when `acc` (the earlier K
+// into float-float values and added to hi + lo (zero, or the earlier K
 // chunks of the tile).  Levels 0-2 enter through exact two-sums; levels 3-5
 // (below 2^-21 of the products' magnitude) are first added in FP32, whose
 // rounding (2^-24 of level 3) stays under the error of the 42-bit digits.
 __device__ __forceinline__ void drain_levels(uint32_t tb, uint32_t col, float (&hi)[16],
-                                             float (&lo)[16], bool acc) {
+                                             float (&lo)[16]) {
   float v[3][16];
   umma::tmem_ld16x3(tb + 3 * kNTile + col, tb + 4 * kNTile + col, tb + 5 * kNTile + col, v);
   float t[16];
@@ -178,7 +183,7 @@ __device__ __forceinline__ void drain_levels(uint32_t tb, uint32_t col, float (&
   umma::tmem_ld16x3(tb + col, tb + kNTile + col, tb + 2 * kNTile + col, v);
 #pragma unroll
   for (int n = 0; n < 16; ++n) {
-    float s = acc ? hi[n] : 0.f, e = acc ? lo[n] : 0.f;
+    float s = hi[n], e = lo[n];
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
       float u, d;
@@ -245,7 +250,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int rank = (int)umma::cluster_ctarank();
   const int cl = blockIdx.x / kCluster;
-  const int beg = sched.slot_off[cl], end = sched.slot_off[cl + 1];
+  int beg = sched.slot_off[cl];
+  const int end = sched.slot_off[cl + 1];
 
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) {
@@ -254,6 +260,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     umma::mbar_init(&B->tfull, 1);
     umma::mbar_init(&B->tempty, kEpiWarps);
+    umma::mbar_init(&B->hfull, 2);
+    umma::mbar_init(&B->hempty, kHelpWarps);
     umma::mbar_init(&B->done, 1);
     B->fail = 0;
     umma::fence_barrier_init();
@@ -370,17 +378,35 @@ __global__ void __launch_bounds__(kThreads, 1)
     warp_wait(&B->done, 0);
   } else {
     // ------------------------------------------------------------ epilogue
-    const int q4 = warp & 3;                   // TMEM lane quarter this warp may access
-    const int c0 = ((warp - 2) >> 2) * 2;      // first of this warp's two 16-column chunks
-    const int row = q4 * 32 + lane;
+    // Work comes in units (TMEM lane quarter qq, 16-column chunk c).  Warps
+    // 2-9 drain: warp w quarter w % 4, chunks c0 and c0 + 1 (columns
+    // 32 ((w - 2) / 4) .. +31).  In the density GEMM, whose units are heavy,
+    // the two quarter-1 warps, which share their SM sub-partition with the
+    // MMA warp, only drain and hand their chunks over in shared memory to
+    // warps 10 (chunks 0, 1) and 11 (chunks 2, 3) on other sub-partitions, so
+    // that the MMA warp keeps its issue slots.  The VXC units are light:
+    // every draining warp processes its own and warps 10-11 stay idle.
+    const bool relays = EPI == EPI_X;
+    const bool helper = warp >= 2 + kEpiWarps;
+    const int q4 = warp & 3;  // TMEM lane quarter this warp may access (draining warps)
+    const int c0 = helper ? (warp - 2 - kEpiWarps) * 2 : ((warp - 2) >> 2) * 2;
+    const bool relay = relays && !helper && q4 == 1;
     const uint32_t lane_base = tmem + ((uint32_t)(q4 * 32) << 16);
-    double* red = reinterpret_cast<double*>(smem + kStages * kStageBytes) + (warp - 2) * 32 * kEpiStride;
+    // one chunk of 32 x 16 values: (hi, lo) floats or doubles, in a layout
+    // of 16 words per row whose column is XOR-swizzled by the row
+    float2* hand = reinterpret_cast<float2*>(smem + kHandOffset);
+    float2* mine = helper || relay ? nullptr
+                   : q4 == 1       ? hand + ((warp - 2) >> 2) * (kChunkBytes / 8)
+                                   : reinterpret_cast<float2*>(smem + kRedOffset) +
+                                         ((warp - 2) - (warp >= 6 ? 1 : 0)) * (kChunkBytes / 8);
+    if (helper && !relays) beg = end;  // nothing to do
     const int nq = gga ? 4 : 1;
-    int li = 0;
+    int li = 0, hn = 0;
     // D of the tile in hand (float-float), summed over its K chunks when the
-    // next entry continues the same tile (density)
+    // next entry continues the same tile (density); zero after each use
     float hi[2][16], lo[2][16];
-    bool acc = false;
+#pragma unroll
+    for (int n = 0; n < 16; ++n) hi[0][n] = lo[0][n] = hi[1][n] = lo[1][n] = 0.f;
     OzItem nit = beg < end ? sched.items[(int64_t)beg * kCluster + rank] : OzItem{};
     for (int sl = beg; sl < end; ++sl) {
       if (warp_failed(B)) break;
@@ -391,90 +417,122 @@ __global__ void __launch_bounds__(kThreads, 1)
       const int lc = li++;
       const bool last = EPI == EPI_V || sl + 1 == end || nit.pb != it.pb || nit.m0 != it.m0 ||
                         nit.n0 != it.n0 || nit.k0 != it.k1;
-      // Tile prologue, before the accumulators are ready: metadata, scales
-      // and global indices.
+      // Tile prologue, before the accumulators are ready: block metadata.
       const int b = it.pb;
       const PBDims d(tk.npts_pad[b], tk.nbe[b]);
       const PBF64 o(d, nq);
       const double* base = f64 + mp.f64_off[b];
-      const int i = it.m0 + row;               // tile row (basis function nu / mu)
-      const int jl = it.n0 + c0 * 16 + lane;   // this lane's column of the warp's 32
-      int e_row = 0, e_col = 0, gm_l = 0, gn_l = 0, ecz = 0;
       int64_t gpt = 0;
-      const float2* phi2 = nullptr;
-      float2 pf[16];  // phi[nu = i][p] of the pass in hand, float-float
+      const int* bfl = nullptr;
+      int ecz = 0;
       if (EPI == EPI_X) {
-        e_row = exp_of_pow2(base[o.r + i]);
-        e_col = exp_of_pow2(base[o.sp + jl]);
         gpt = tk.pt_off[b] + it.n0;
-        phi2 = reinterpret_cast<const float2*>(base + o.phi2) + i;
       } else {
-        const int* bfl = tk.bf_list + tk.bf_off[b];
-        gm_l = bfl[i];
-        gn_l = bfl[jl];
+        bfl = tk.bf_list + tk.bf_off[b];
         ecz = exp_of_pow2(base[o.cz]);
       }
-      if (!warp_wait(&B->tfull, lc & 1)) {
-        if (lane == 0) set_fail(B, ERR_TFULL);
-        break;
+      if (!helper) {
+        if (!warp_wait(&B->tfull, lc & 1)) {
+          if (lane == 0) set_fail(B, ERR_TFULL);
+          break;
+        }
+        umma::fence_after_sync();
+        // levels -> float-float in registers, then TMEM goes back to the MMAs
+        drain_levels(lane_base, c0 * 16, hi[0], lo[0]);
+        drain_levels(lane_base, c0 * 16 + 16, hi[1], lo[1]);
+        umma::fence_before_sync();
+        __syncwarp();
+        if (lane == 0) umma::mbar_arrive(&B->tempty);
       }
-      umma::fence_after_sync();
-      // levels -> float-float in registers, then TMEM goes back to the MMAs
-      drain_levels(lane_base, c0 * 16, hi[0], lo[0], acc);
-      drain_levels(lane_base, c0 * 16 + 16, hi[1], lo[1], acc);
-      umma::fence_before_sync();
-      __syncwarp();
-      if (lane == 0) umma::mbar_arrive(&B->tempty);
-      acc = !last;
       if (!last) continue;
-      if (EPI == EPI_X) {
-        const float2* f = phi2 + (int64_t)(it.n0 + c0 * 16) * d.nu128;
+      const int hc = hn++;
+      auto put = [&](float2* buf, const float (&h0)[16], const float (&l0)[16]) {
 #pragma unroll
-        for (int n = 0; n < 16; ++n) pf[n] = f[(int64_t)n * d.nu128];
-        // the second column chunk waits in shared memory (registers)
-        float* park = reinterpret_cast<float*>(red);
+        for (int n = 0; n < 16; ++n) buf[lane * 16 + (n ^ (lane & 15))] = make_float2(h0[n], l0[n]);
+      };
+      auto get = [&](const float2* buf, float (&h0)[16], float (&l0)[16]) {
 #pragma unroll
         for (int n = 0; n < 16; ++n) {
-          park[n * 32 + lane] = hi[1][n];
-          park[(16 + n) * 32 + lane] = lo[1][n];
+          const float2 v = buf[lane * 16 + (n ^ (lane & 15))];
+          h0[n] = v.x;
+          l0[n] = v.y;
         }
-      }
-      if (EPI == EPI_X) {
-        // passes (k, q): column chunk c0 + k, value q (phi, then 2 grad phi)
+      };
+      auto clear = [&](float (&h0)[16], float (&l0)[16]) {
 #pragma unroll
-        for (int k = 0; k < 2; ++k) {
-          const int c = c0 + k;
-          if (k == 1) {
-            const float* park = reinterpret_cast<const float*>(red);
+        for (int n = 0; n < 16; ++n) h0[n] = l0[n] = 0.f;
+      };
+      if (relay) {
+        // hand both chunks over once the helpers are done with the previous ones
+        if (hc >= 1 && !warp_wait(&B->hempty, (hc - 1) & 1)) {
+          if (lane == 0) set_fail(B, ERR_HAND);
+          break;
+        }
+        put(hand + (c0 + 0) * (kChunkBytes / 8), hi[0], lo[0]);
+        put(hand + (c0 + 1) * (kChunkBytes / 8), hi[1], lo[1]);
+        __syncwarp();
+        if (lane == 0) umma::mbar_arrive(&B->hfull);
+        clear(hi[0], lo[0]);
+        clear(hi[1], lo[1]);
+        continue;
+      }
+      if (helper && !warp_wait(&B->hfull, hc & 1)) {
+        if (lane == 0) set_fail(B, ERR_HAND);
+        break;
+      }
+      // density: the second chunk waits in shared memory while the first is
+      // processed (registers); VXC keeps it and uses `mine` to transpose
+      if (!helper && EPI == EPI_X) put(mine, hi[1], lo[1]);
+      float2* scratch = helper ? hand + c0 * (kChunkBytes / 8) : mine;
+      for (int k = 0; k < 2; ++k) {
+        const int c = c0 + k;
+        const int qq = helper ? 1 : q4;
+        if (helper) {
+          get(hand + c * (kChunkBytes / 8), hi[0], lo[0]);
+        } else if (k == 1) {
+          if (EPI == EPI_X) {
+            get(mine, hi[0], lo[0]);
+          } else {
 #pragma unroll
             for (int n = 0; n < 16; ++n) {
-              hi[1][n] = park[n * 32 + lane];
-              lo[1][n] = park[(16 + n) * 32 + lane];
+              hi[0][n] = hi[1][n];
+              lo[0][n] = lo[1][n];
             }
           }
+        }
+        __syncwarp();
+        // one unit: rows of quarter qq, columns jc .. jc + 15, values hi[0] + lo[0]
+        const int i = it.m0 + qq * 32 + lane;  // tile row (basis function nu / mu)
+        const int jc = it.n0 + c * 16;
+        if (EPI == EPI_X) {
           // X'[nu, p] = 2^(er + esp - 13) D, a power of two times D
+          const int e_row = exp_of_pow2(base[o.r + i]);
+          const int e_col = exp_of_pow2(base[o.sp + jc + (lane & 15)]);
+          const float2* ph = reinterpret_cast<const float2*>(base + o.phi2) + i + (int64_t)jc * d.nu128;
+          float2 pf[16];  // phi[nu = i][p] of the pass in hand, float-float
+#pragma unroll
+          for (int n = 0; n < 16; ++n) pf[n] = ph[(int64_t)n * d.nu128];
 #pragma unroll
           for (int n = 0; n < 16; ++n) {
-            const float sc = ff::pow2f(e_row + __shfl_sync(0xffffffffu, e_col, 16 * k + n) - 13);
-            hi[k][n] *= sc;
-            lo[k][n] *= sc;
+            const float sc = ff::pow2f(e_row + __shfl_sync(0xffffffffu, e_col, n) - 13);
+            hi[0][n] *= sc;
+            lo[0][n] *= sc;
           }
+          // passes q: phi, then 2 grad phi
           for (int q = 0; q < nq; ++q) {
             float h[16], l[16];
 #pragma unroll
             for (int n = 0; n < 16; ++n) {
               float2 fv = pf[n];
               if (q) fv = make_float2(2.f * fv.x, 2.f * fv.y);
-              const float2 t = ff::mul(make_float2(hi[k][n], lo[k][n]), fv);
+              const float2 t = ff::mul(make_float2(hi[0][n], lo[0][n]), fv);
               h[n] = t.x;
               l[n] = t.y;
             }
             // the next pass's phi values load while this pass is reduced
-            if (q + 1 < nq || k == 0) {
-              const int qn = q + 1 < nq ? q + 1 : 0, cn = q + 1 < nq ? c : c + 1;
-              const float2* f = phi2 + qn * o.blk + (int64_t)(it.n0 + cn * 16) * d.nu128;
+            if (q + 1 < nq) {
 #pragma unroll
-              for (int n = 0; n < 16; ++n) pf[n] = f[(int64_t)n * d.nu128];
+              for (int n = 0; n < 16; ++n) pf[n] = ph[(q + 1) * o.blk + (int64_t)n * d.nu128];
             }
             reduce16(h, l, lane);
             if ((lane & 1) == 0) {
@@ -483,32 +541,39 @@ __global__ void __launch_bounds__(kThreads, 1)
               atomicAdd(&out[4 * (gpt + c * 16 + n) + q], ff::to_double_fast(h[0], l[0], 0));
             }
           }
-        }
-      } else {
-        // S[i][j] = (phi^T Z + Z^T phi)[i][j] = 2^(ecz - 14) D: the strict
-        // upper triangle (i < j, union indices) goes to A[i][j], the diagonal
-        // as S[i][i] / 2, so that A + A^T is the block's VXC contribution.
-#pragma unroll
-        for (int k = 0; k < 2; ++k) {
-          const int j0 = it.n0 + (c0 + k) * 16;
+        } else {
+          // S[i][j] = (phi^T Z + Z^T phi)[i][j] = 2^(ecz - 14) D: the strict
+          // upper triangle (i < j, union indices) goes to A[i][j], the
+          // diagonal as S[i][i] / 2, so that A + A^T is the block's VXC
+          // contribution.  Transposed through `scratch` (as doubles) for
+          // atomics along rows of A.
+          const int gm_l = bfl[i];
+          const int gn_l = bfl[jc + (lane & 15)];
+          double* tr = reinterpret_cast<double*>(scratch);
 #pragma unroll
           for (int n = 0; n < 16; ++n)
-            red[lane * kEpiStride + n] =
-                i <= j0 + n ? ff::to_double_fast(hi[k][n], lo[k][n], ecz - 14 - (i == j0 + n ? 1 : 0))
+            tr[lane * 16 + (n ^ (lane & 15))] =
+                i <= jc + n ? ff::to_double_fast(hi[0][n], lo[0][n], ecz - 14 - (i == jc + n ? 1 : 0))
                             : 0.;
           __syncwarp();
           const int n = lane & 15;
-          const int gn = __shfl_sync(0xffffffffu, gn_l, 16 * k + n);
+          const int gn = __shfl_sync(0xffffffffu, gn_l, n);
 #pragma unroll
           for (int t = 0; t < 16; ++t) {
             const int r2 = (lane >> 4) + 2 * t;
-            const int im = it.m0 + q4 * 32 + r2;
+            const int im = it.m0 + qq * 32 + r2;
             const int gm = __shfl_sync(0xffffffffu, gm_l, r2);
-            if (im <= j0 + n && gm >= 0 && gn >= 0)
-              atomicAdd(&out[(int64_t)gm * nbf + gn], red[r2 * kEpiStride + n]);
+            if (im <= jc + n && gm >= 0 && gn >= 0)
+              atomicAdd(&out[(int64_t)gm * nbf + gn], tr[r2 * 16 + (n ^ (r2 & 15))]);
           }
           __syncwarp();
         }
+        clear(hi[0], lo[0]);
+      }
+      clear(hi[1], lo[1]);
+      if (helper) {
+        __syncwarp();
+        if (lane == 0) umma::mbar_arrive(&B->hempty);
       }
     }
   }
