@@ -484,6 +484,9 @@ def main():
         roofline = dict(bound="tensor", kernel=f"ozaki_kernel<{'X' if dom == 'density' else 'V'}>",
                         achieved=achieved, peak=peak, unit="TFLOP/s", frac=achieved / peak,
                         traffic=traffic, peak_source=src,
+                        traffic_note=("DRAM read+write bytes per launch (ncu launch list, "
+                                      "profiles/launches_mixed_256water.md)" if traffic else None),
+                        launches_per_step=kt[dom]["launches"] / args.steps,
                         algorithmic_flops_per_step=tflops / args.steps,
                         fp64_equivalent_tflops=f64_flops / dom_s / 1e12)
     else:
