@@ -167,7 +167,8 @@ class DeviceIntegrator {
   PBMaskDev mk_{};
   MixedPBDev mp_{};
   std::vector<MBatch> mbatches_;
-  OzItem* slots_ = nullptr;  // GEMM slots of every launch (kCluster tiles each)
+  OzItem* slots_ = nullptr;
+  std::vector<int> zoff_h_;   // host copy of MixedPBDev::zoff  // GEMM slots of every launch (kCluster tiles each)
   int* sched_ = nullptr;
   double* f64_ = nullptr;
   __nv_bfloat16* dig_ = nullptr;
@@ -617,6 +618,13 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
   mk_.mask = arena_.upload(mask, s);
   mp_.f64_off = tk_.scr_off;
   mp_.dig_off = arena_.upload(dig_off, s);
+  // z_digits CTAs: nu128 np / 2048 per block (256 threads, 8 points each)
+  zoff_h_.assign(npb + 1, 0);
+  for (int i = 0; i < npb; ++i) {
+    const PBDims d(npts_pad[i], nu[i]);
+    zoff_h_[i + 1] = zoff_h_[i] + d.nu128 * d.np / 2048;
+  }
+  mp_.zoff = arena_.upload(zoff_h_, s);
   coll_items_ = arena_.upload(coll, s);
   slots_ = arena_.upload(slots, s);
   sched_ = arena_.upload(sched, s);
@@ -660,8 +668,8 @@ int64_t DeviceIntegrator::eval_mixed_batches(bool do_vxc) {
     });
     if (!do_vxc) continue;
     launches += timed(2, [&] {
-      launch_z_digits(tk_, mp_, b.b0, b.b1, b.max_nu_pad, gga_, zcoef_, f64_, dig_, s);
-      return (int64_t)1;
+      launch_z_digits(tk_, mp_, b.b0, b.b1, zoff_h_[b.b0], zoff_h_[b.b1], gga_, zcoef_, f64_, dig_, s);
+      return (int64_t)2;
     });
     launches += timed(3, [&] {
       launch_ozaki_v(tk_, mp_, OzSchedule{slots_, sched_ + b.v_sched, b.v_ncl}, f64_, dig_, gga_,

@@ -1,12 +1,13 @@
 // Tensor-core GEMMs of the mixed-precision path (tcgen05.mma, BF16 digits,
 // FP32 level accumulators in TMEM) with two fused epilogues:
 //
-//  X tile (density): D[nu, p] = sum_mu Pd[nu, mu] Fd[p, mu] over one K chunk;
-//    X'[nu, p] = 2 * 2^-14 * D * r_nu * s_p is contracted on the spot with
-//    phi[nu, p] (rho) and 2 grad phi[nu, p] (grad rho); the sums over the
-//    tile's 128 basis rows (TMEM lanes) run as warp reduce-scatters in
+//  X tile (density): D[nu, p] = sum_mu Pd[nu, mu] Fd[p, mu], K chunks of
+//    <= 512 run back to back on one CTA and are summed in float-float
+//    registers; X'[nu, p] = 2 * 2^-14 * D * r_nu * s_p is then contracted
+//    with phi[nu, p] (rho) and 2 grad phi[nu, p] (grad rho); the sums over
+//    the tile's 128 basis rows (TMEM lanes) run as warp reduce-scatters in
 //    float-float arithmetic and each warp adds its per-point partials to
-//    rho4.  rho is linear in X, so K chunks never need to be summed in X.
+//    rho4.
 //  V tile (VXC): D[mu, nu] = sum_k Va[mu, k] Vb[nu, k] over K = 2 np, i.e.
 //    (phi^T Z + Z^T phi)[mu, nu] / cz; only tiles reaching the upper triangle
 //    run, and A[mu, nu] += 2^-14 cz D for mu < nu (half of it for mu = nu),
@@ -38,7 +39,9 @@
 //             32 ((w - 2) / 4) .. +31 of each level.  The six levels of a
 //             column are summed into a float-float value right away, TMEM is
 //             handed back (`tempty`) and the rest of the epilogue runs from
-//             registers while the next tile's MMAs proceed.
+//             registers while the next tile's MMAs proceed;
+//   warps 10-11 (density only) process the chunks that warps 5 and 9, which
+//             share the MMA warp's SM sub-partition, drain and hand over.
 // Every mbarrier wait is bounded.  On expiry the CTA records an error code,
 // each role leaves its loop, the producer waits (bounded) until the cluster
 // has released the stages it filled, the MMA lane for its MMAs, TMEM is
@@ -168,11 +171,14 @@ __device__ __forceinline__ void reduce16(float (&h)[16], float (&l)[16], int lan
   l[0] = t.y;
 }
 
-// This thread's lane of TMEM columns [col, col + 16) of the six levels, summed
-// into float-float values and added to hi + lo (zero, or the earlier K
-// chunks of the tile).  Levels 0-2 enter through exact two-sums; levels 3-5
-// (below 2^-21 of the products' magnitude) are first added in FP32, whose
-// rounding (2^-24 of level 3) stays under the error of the 42-bit digits.
+// This thread's lane of TMEM columns [col, col + 16) of the six levels as
+// float-float values hi + lo; ACC: added to hi + lo (the earlier K chunks of
+// the tile).  Levels 0-2 (and the running sum) enter through exact two-sums;
+// levels 3-5 (below 2^-21 of the products' magnitude) are summed in FP32 and
+// added to lo with the two-sums' error terms, whose rounding (2^-24 of level
+// 3) stays under the error of the 42-bit digits; a final fast two-sum
+// normalises hi + lo.
+template <bool ACC>
 __device__ __forceinline__ void drain_levels(uint32_t tb, uint32_t col, float (&hi)[16],
                                              float (&lo)[16]) {
   float v[3][16];
@@ -183,16 +189,20 @@ __device__ __forceinline__ void drain_levels(uint32_t tb, uint32_t col, float (&
   umma::tmem_ld16x3(tb + col, tb + kNTile + col, tb + 2 * kNTile + col, v);
 #pragma unroll
   for (int n = 0; n < 16; ++n) {
-    float s = hi[n], e = lo[n];
-#pragma unroll
-    for (int a = 0; a < 4; ++a) {
-      float u, d;
-      ff::two_sum(s, a < 3 ? v[a][n] : t[n], u, d);
-      s = u;
-      e += d;
+    float s, e, u, d;
+    if (ACC) {
+      ff::two_sum(hi[n], v[0][n], s, e);
+      e += lo[n];
+    } else {
+      s = v[0][n];
+      e = 0.f;
     }
-    hi[n] = s;
-    lo[n] = e;
+    ff::two_sum(s, v[1][n], u, d);
+    e += d;
+    ff::two_sum(u, v[2][n], s, d);
+    const ff::ffl r = ff::fast_two_sum(s, e + (d + t[n]));  // |lo| <= ulp(hi) / 2
+    hi[n] = r.hi;
+    lo[n] = r.lo;
   }
 }
 
@@ -405,6 +415,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     // D of the tile in hand (float-float), summed over its K chunks when the
     // next entry continues the same tile (density); zero after each use
     float hi[2][16], lo[2][16];
+    bool acc = false;  // hi + lo hold the earlier K chunks of the tile
 #pragma unroll
     for (int n = 0; n < 16; ++n) hi[0][n] = lo[0][n] = hi[1][n] = lo[1][n] = 0.f;
     OzItem nit = beg < end ? sched.items[(int64_t)beg * kCluster + rank] : OzItem{};
@@ -438,12 +449,18 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         umma::fence_after_sync();
         // levels -> float-float in registers, then TMEM goes back to the MMAs
-        drain_levels(lane_base, c0 * 16, hi[0], lo[0]);
-        drain_levels(lane_base, c0 * 16 + 16, hi[1], lo[1]);
+        if (acc) {
+          drain_levels<true>(lane_base, c0 * 16, hi[0], lo[0]);
+          drain_levels<true>(lane_base, c0 * 16 + 16, hi[1], lo[1]);
+        } else {
+          drain_levels<false>(lane_base, c0 * 16, hi[0], lo[0]);
+          drain_levels<false>(lane_base, c0 * 16 + 16, hi[1], lo[1]);
+        }
         umma::fence_before_sync();
         __syncwarp();
         if (lane == 0) umma::mbar_arrive(&B->tempty);
       }
+      acc = EPI == EPI_X && !last;
       if (!last) continue;
       const int hc = hn++;
       auto put = [&](float2* buf, const float (&h0)[16], const float (&l0)[16]) {

@@ -137,13 +137,15 @@ __global__ void phi_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const doub
     store_digits8(x, es, v.Va + oz_offset(0, mu, p0, kMTile, k2), kMTile * kBK);
     if (mu < d.nun) store_digits8(x, es, v.Vb + oz_offset(0, mu, d.np + p0, kNTile, k2), kNTile * kBK);
   }
-  const int p = threadIdx.x;
-  if (p >= d.np) return;
+  // transposition: thread (point p, sub-lane sub) takes every nsub-th row
+  // group of this CTA's share, so that small blocks keep all threads busy
+  const int nsub = blockDim.x / d.np, sub = threadIdx.x / d.np, p = threadIdx.x % d.np;
+  if (sub >= nsub) return;
   const int ng = d.nu128 / 8;
   const int per = (ng + gridDim.x - 1) / gridDim.x;
   const int g0 = blockIdx.x * per, g1 = min(ng, g0 + per);
   unsigned gmax = 0;
-  for (int g = g0; g < g1; ++g) {
+  for (int g = g0 + sub; g < g1; g += nsub) {
     const int mu0 = g * 8;
     for (int q = 0; q < nq; ++q) {
       ffl x[8];
@@ -232,19 +234,16 @@ __global__ void p_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const double
 // Zt[nu][p] = sp[p] (zc.x phi + zc.y dphi_x + zc.z dphi_y + zc.w dphi_z),
 // in float-float, with one scale cz for the whole block: 2^e above the bound
 //   |Zt| <= sp (|zc.x| sp + (|zc.y| + |zc.z| + |zc.w|) max|grad phi|)
-// taken from exponents only.  Digits go to Vb[nu][p] (rows nu < nun) and
-// Va[nu][np + p] (rows nu < nu128).  One CTA per 8 rows nu; thread (row
-// tid & 7, point group tid >> 3).
-__global__ void z_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const double4* __restrict__ zc,
-                                double* f64, __nv_bfloat16* dig, int gga) {
+// taken from exponents only (z_scale_kernel, one CTA per block).  Digits go
+// to Vb[nu][p] (rows nu < nun) and Va[nu][np + p] (rows nu < nu128).
+__global__ void z_scale_kernel(TasksDev tk, MixedPBDev mp, int b0, const double4* __restrict__ zc,
+                               double* f64, int gga) {
   __shared__ int red[32];
-  const int b = b0 + blockIdx.y;
-  PBView v(tk, mp, b, gga, f64, dig);
+  const int b = b0 + blockIdx.x;
+  PBView v(tk, mp, b, gga, f64, nullptr);
   const PBDims& d = v.d;
-  if (blockIdx.x * 8 >= d.nu128) return;
   // coefficients of point p: zf[4 p + k], float-float (functional_kernel)
   const ffl* zf = reinterpret_cast<const ffl*>(zc + tk.pt_off[b]);
-  // block scale: max over points of the exponent bound
   int eb = -1000;
   for (int p = threadIdx.x; p < d.np; p += blockDim.x) {
     const int esp = exp_of_pow2(v.sp[p]);
@@ -264,29 +263,66 @@ __global__ void z_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const double
   int es_z = -1000;
   for (int k = 0; k < (int)(blockDim.x >> 5); ++k) es_z = max(es_z, red[k]);
   es_z = min(max(es_z, -1000), 1000);
-  const int row = blockIdx.x * 8 + (threadIdx.x & 7);
-  if (threadIdx.x < 8) v.cz[row] = ff::pow2(es_z);
-  const int ng = d.np / 8, step = blockDim.x / 8;
+  const double cz = ff::pow2(es_z);
+  for (int row = threadIdx.x; row < d.nu128; row += blockDim.x) v.cz[row] = cz;
+  // the point scale sp (a power of two) folds exactly into the coefficients
+  ffl* zw = reinterpret_cast<ffl*>(const_cast<double4*>(zc) + tk.pt_off[b]);
+  for (int p = threadIdx.x; p < d.np; p += blockDim.x) {
+    const int esp = exp_of_pow2(v.sp[p]);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) zw[4 * p + k] = scale2(zf[4 * p + k], esp);
+  }
+}
+
+// One thread per (row nu, 8-point group): CTA c of the launch covers pairs
+// 256 (c - zoff[b]) .. +255 of block b (zoff: CTA offsets of the blocks,
+// nu128 np / 2048 each), rows in groups of 8 with the point group next, so
+// that 8 lanes write one 128-byte core matrix.
+__global__ void z_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, int b1, int c0,
+                                const double4* __restrict__ zc, double* f64, __nv_bfloat16* dig,
+                                int gga) {
+  const int c = c0 + blockIdx.x;
+  int lo = b0, hi = b1 - 1;  // last block with zoff[b] <= c
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (mp.zoff[mid] <= c) lo = mid; else hi = mid - 1;
+  }
+  const int b = lo;
+  PBView v(tk, mp, b, gga, f64, dig);
+  const PBDims& d = v.d;
+  const int ng = d.np / 8;
+  const int t = (c - mp.zoff[b]) * blockDim.x + threadIdx.x;
+  const int row = (t / (8 * ng)) * 8 + (t & 7), g = (t % (8 * ng)) >> 3;
+  if (row >= d.nu128) return;
+  // coefficients already scaled by sp (z_scale_kernel): 4 float-float per point
+  const float4* zf4 = reinterpret_cast<const float4*>(zc + tk.pt_off[b]) + 2 * (g * 8);
+  const int es_z = exp_of_pow2(v.cz[0]);
   const int k2 = 2 * d.np;
-  const ffl* f = v.phi + (int64_t)row * d.np;
-  // Zt in float-float; the point scale is an exact power of two
-  auto zval = [&](int p) {
-    ffl val = zf[4 * p] * f[p];
-    if (gga)
-      val = val + zf[4 * p + 1] * f[p + v.o.blk] + zf[4 * p + 2] * f[p + 2 * v.o.blk] +
-            zf[4 * p + 3] * f[p + 3 * v.o.blk];
-    return scale2(val, exp_of_pow2(v.sp[p]));
-  };
+  // Zt in float-float, 16-byte loads: phi of 8 points is 4 float4 per value q
+  const float4* f4 = reinterpret_cast<const float4*>(v.phi + (int64_t)row * d.np + g * 8);
+  const int64_t qs = v.o.blk / 2;  // one value plane, in float4
+  ffl x[8];
+#pragma unroll
+  for (int e2 = 0; e2 < 4; ++e2) {
+    const float4 c0 = zf4[4 * e2], c1 = zf4[4 * e2 + 1], c2 = zf4[4 * e2 + 2], c3 = zf4[4 * e2 + 3];
+    const float4 ph = f4[e2];
+    ffl v0 = ffl(c0.x, c0.y) * ffl(ph.x, ph.y);
+    ffl v1 = ffl(c2.x, c2.y) * ffl(ph.z, ph.w);
+    if (gga) {
+      const float4 gx = f4[qs + e2], gy = f4[2 * qs + e2], gz = f4[3 * qs + e2];
+      v0 = v0 + ffl(c0.z, c0.w) * ffl(gx.x, gx.y) + ffl(c1.x, c1.y) * ffl(gy.x, gy.y) +
+           ffl(c1.z, c1.w) * ffl(gz.x, gz.y);
+      v1 = v1 + ffl(c2.z, c2.w) * ffl(gx.z, gx.w) + ffl(c3.x, c3.y) * ffl(gy.z, gy.w) +
+           ffl(c3.z, c3.w) * ffl(gz.z, gz.w);
+    }
+    x[2 * e2] = v0;
+    x[2 * e2 + 1] = v1;
+  }
   int es[8];
 #pragma unroll
   for (int e = 0; e < 8; ++e) es[e] = es_z;
-  for (int g = threadIdx.x >> 3; g < ng; g += step) {
-    ffl x[8];
-#pragma unroll
-    for (int e = 0; e < 8; ++e) x[e] = zval(g * 8 + e);
-    store_digits8(x, es, v.Va + oz_offset(0, row, d.np + g * 8, kMTile, k2), kMTile * kBK);
-    if (row < d.nun) store_digits8(x, es, v.Vb + oz_offset(0, row, g * 8, kNTile, k2), kNTile * kBK);
-  }
+  store_digits8(x, es, v.Va + oz_offset(0, row, d.np + g * 8, kMTile, k2), kMTile * kBK);
+  if (row < d.nun) store_digits8(x, es, v.Vb + oz_offset(0, row, g * 8, kNTile, k2), kNTile * kBK);
 }
 
 // ---------------------------------------------------------------- functional
@@ -359,12 +395,13 @@ void launch_p_digits(const TasksDev& tk, const MixedPBDev& mp, int b0, int b1, i
   GB300_CUDA(cudaGetLastError());
 }
 
-void launch_z_digits(const TasksDev& tk, const MixedPBDev& mp, int b0, int b1, int max_nu_pad,
+void launch_z_digits(const TasksDev& tk, const MixedPBDev& mp, int b0, int b1, int zc0, int zc1,
                      bool gga, const double4* zcoef, double* f64, __nv_bfloat16* dig,
                      cudaStream_t s) {
-  if (b1 <= b0) return;
-  z_digits_kernel<<<dim3(max_nu_pad / 8, b1 - b0), 256, 0, s>>>(tk, mp, b0, zcoef, f64, dig,
-                                                                 gga);
+  if (b1 <= b0 || zc1 <= zc0) return;
+  z_scale_kernel<<<b1 - b0, 256, 0, s>>>(tk, mp, b0, zcoef, f64, gga);
+  GB300_CUDA(cudaGetLastError());
+  z_digits_kernel<<<zc1 - zc0, 256, 0, s>>>(tk, mp, b0, b1, zc0, zcoef, f64, dig, gga);
   GB300_CUDA(cudaGetLastError());
 }
 

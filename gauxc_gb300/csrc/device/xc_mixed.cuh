@@ -92,6 +92,7 @@ struct PBMaskDev {
 struct MixedPBDev {
   const int64_t* f64_off;   // doubles: PBF64 layout
   const int64_t* dig_off;   // bf16 elements: PBDims layout
+  const int* zoff;          // first z_digits CTA of each block (nu128 np / 2048 per block)
 };
 
 // One tensor-core GEMM tile: output rows [m0, m0+128) x cols [n0, n0+64),
@@ -138,7 +139,8 @@ void launch_p_row_scales(const double* P, int nbf, double* rs, cudaStream_t s);
 void launch_p_digits(const TasksDev& tk, const MixedPBDev& mp, int b0, int b1, int max_nu_pad,
                      bool gga, const double* P, const double* rs, int nbf, double* f64,
                      __nv_bfloat16* dig, cudaStream_t s);
-void launch_z_digits(const TasksDev& tk, const MixedPBDev& mp, int b0, int b1, int max_nu_pad,
+// Z digits of blocks [b0, b1), whose z_digits CTAs are [zc0, zc1) (MixedPBDev::zoff).
+void launch_z_digits(const TasksDev& tk, const MixedPBDev& mp, int b0, int b1, int zc0, int zc1,
                      bool gga, const double4* zcoef, double* f64, __nv_bfloat16* dig,
                      cudaStream_t s);
 // Functional on points [g0, g1): zcoef and functional_partial_blocks() EXC/N_el partials.
