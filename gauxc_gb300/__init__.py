@@ -404,9 +404,9 @@ class XCIntegrator(_Handle):
         _call(_L.gauxc_gb300_integrator_set_profiling, self._h, ctypes.c_bool(on))
 
     def kernel_times(self):
-        out = (ctypes.c_double * 10)()
-        _call(_L.gauxc_gb300_integrator_kernel_times, self._h, out, 10)
-        names = ["collocation", "density", "zmat", "vxc", "other"]
+        out = (ctypes.c_double * 14)()
+        _call(_L.gauxc_gb300_integrator_kernel_times, self._h, out, 14)
+        names = ["collocation", "density", "zmat", "vxc", "other", "phi_digits", "p_digits"]
         return {n: dict(ms=out[2 * i], launches=int(out[2 * i + 1])) for i, n in enumerate(names)}
 
     def plan_stats(self):

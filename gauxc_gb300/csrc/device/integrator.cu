@@ -119,8 +119,9 @@ class DeviceIntegrator {
   std::map<std::string, double> timings;
   bool profiling = false;
   // per kernel class: accumulated ms and launch count of the last call
-  double kclass_ms[5] = {0, 0, 0, 0, 0};
-  int64_t kclass_n[5] = {0, 0, 0, 0, 0};
+  // collocation, density, zmat, vxc, other, phi digits (+ point scales), P digits
+  double kclass_ms[7] = {0, 0, 0, 0, 0, 0, 0};
+  int64_t kclass_n[7] = {0, 0, 0, 0, 0, 0, 0};
 
   void eval(const double* P, int64_t ldp, double* VXC, int64_t ldvxc, double* EXC, double* NEL,
             bool den_only);
@@ -651,11 +652,14 @@ int64_t DeviceIntegrator::eval_mixed_batches(bool do_vxc) {
                                 b.coll_end - b.coll_begin, f64_, gga_, s);
       return (int64_t)1;
     });
-    launches += timed(4, [&] {
+    launches += timed(5, [&] {
       launch_point_scales(tk_, mp_, b.b0, b.b1, gga_, f64_, s);
       launch_phi_digits(tk_, mp_, b.b0, b.b1, gga_, f64_, dig_, s);
+      return (int64_t)2;
+    });
+    launches += timed(6, [&] {
       launch_p_digits(tk_, mp_, b.b0, b.b1, b.max_nu_pad, gga_, P_, prs_, nbf_, f64_, dig_, s);
-      return (int64_t)3;
+      return (int64_t)1;
     });
     launches += timed(1, [&] {
       launch_ozaki_x(tk_, mp_, OzSchedule{slots_, sched_ + b.x_sched, b.x_ncl}, f64_, dig_, gga_,
@@ -759,7 +763,7 @@ void DeviceIntegrator::eval(const double* P, int64_t ldp, double* VXC, int64_t l
   timings["d2h_ms"] = d2h;
   timings["wall_ms"] = std::chrono::duration<double, std::milli>(t_host1 - t_host0).count();
   timings["gpu_launches"] = (double)launches;
-  for (int k = 0; k < 5; ++k) {
+  for (int k = 0; k < 7; ++k) {
     kclass_ms[k] = 0.;
     kclass_n[k] = 0;
   }
@@ -827,9 +831,9 @@ void integrator_set_profiling(XCIntegratorHandle& h, bool on) {
 }
 
 std::vector<double> integrator_kernel_times(const XCIntegratorHandle& h) {
-  std::vector<double> v(10, 0.);
+  std::vector<double> v(14, 0.);
   if (!h.dev) return v;
-  for (int k = 0; k < 5; ++k) {
+  for (int k = 0; k < 7; ++k) {
     v[2 * k] = h.dev->kclass_ms[k];
     v[2 * k + 1] = (double)h.dev->kclass_n[k];
   }

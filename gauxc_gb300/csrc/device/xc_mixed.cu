@@ -45,14 +45,6 @@ __device__ __forceinline__ void store_digits8(const T (&x)[8], const int (&es)[8
 
 using ff::ffl;
 
-// float-float scaled by 2^e (exact in the float range)
-__device__ __forceinline__ ffl scale2(ffl v, int e) {
-  const float s = ff::pow2f(e);
-  return ffl(v.hi * s, v.lo * s);
-}
-
-__device__ __forceinline__ unsigned abs_key_f(ffl v) { return __float_as_uint(v.hi) & 0x7FFFFFFFu; }
-
 struct PBView {
   PBDims d;
   PBF64 o;
@@ -278,7 +270,7 @@ __global__ void z_scale_kernel(TasksDev tk, MixedPBDev mp, int b0, const double4
 // 256 (c - zoff[b]) .. +255 of block b (zoff: CTA offsets of the blocks,
 // nu128 np / 2048 each), rows in groups of 8 with the point group next, so
 // that 8 lanes write one 128-byte core matrix.
-__global__ void z_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, int b1, int c0,
+__global__ void __launch_bounds__(256, 4) z_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, int b1, int c0,
                                 const double4* __restrict__ zc, double* f64, __nv_bfloat16* dig,
                                 int gga) {
   const int c = c0 + blockIdx.x;

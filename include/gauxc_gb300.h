@@ -264,7 +264,8 @@ int gauxc_gb300_integrator_plan_stats(GauXCStatus* status, const GauXCIntegrator
 void gauxc_gb300_integrator_set_profiling(GauXCStatus* status, const GauXCIntegrator integrator,
                                           bool on);
 /* {collocation ms, launches, density ms, launches, zmat ms, launches, vxc ms,
-   launches, other ms, launches} of the last call; returns the count written. */
+   launches, other ms, launches, phi digits ms, launches, P digits ms, launches}
+   of the last call (at most nmax values); returns the count written. */
 int gauxc_gb300_integrator_kernel_times(GauXCStatus* status, const GauXCIntegrator integrator,
                                         double* out, int nmax);
 /* Measured FP64 FMA throughput of the current device in TFLOP/s (about 50 ms probe). */
