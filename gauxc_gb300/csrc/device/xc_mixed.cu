@@ -45,6 +45,14 @@ __device__ __forceinline__ void store_digits8(const T (&x)[8], const int (&es)[8
 
 using ff::ffl;
 
+// float-float scaled by 2^e (exact in the float range)
+__device__ __forceinline__ ffl scale2(ffl v, int e) {
+  const float s = ff::pow2f(e);
+  return ffl(v.hi * s, v.lo * s);
+}
+
+__device__ __forceinline__ unsigned abs_key_f(ffl v) { return __float_as_uint(v.hi) & 0x7FFFFFFFu; }
+
 struct PBView {
   PBDims d;
   PBF64 o;
