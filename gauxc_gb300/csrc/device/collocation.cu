@@ -26,9 +26,25 @@ namespace gb300 {
 
 namespace {
 
-template <bool GRAD, typename V>
-__device__ __forceinline__ void eval_shell(int l, int pure, V x, V y, V z, V R, V R1, V* f, V* fx,
-                                           V* fy, V* fz, int64_t s) {
+// Value sink for the generated angular code: stores a float-float value and
+// keeps the largest |hi| seen, as IEEE magnitude bits, in *m.
+struct MaxSink {
+  ff::ffl* p;
+  unsigned* m;
+  struct Ref {
+    ff::ffl* q;
+    unsigned* m;
+    __device__ __forceinline__ void operator=(ff::ffl v) const {
+      *q = v;
+      *m = max(*m, __float_as_uint(v.hi) & 0x7FFFFFFFu);
+    }
+  };
+  __device__ __forceinline__ Ref operator[](int64_t i) const { return Ref{p + i, m}; }
+};
+
+template <bool GRAD, typename V, typename O>
+__device__ __forceinline__ void eval_shell(int l, int pure, V x, V y, V z, V R, V R1, O f, O fx,
+                                           O fy, O fz, int64_t s) {
   if (GRAD) {
     if (pure) {
       switch (l) {
@@ -97,6 +113,7 @@ __global__ void __launch_bounds__(128) collocation_kernel(ShellsDev sh, TasksDev
   const int ns = tk.nsh[t];
   const uint8_t* active = nullptr;
   if (MASK) active = mk.mask + mk.mask_off[t] + (int64_t)mk.member[g] * ns;
+  unsigned mval = 0, mgrad = 0;  // largest |phi|, |grad phi| of the point (mixed path)
   for (int i = 0; i < ns; ++i) {
     const int s = tk.sh_list[s0 + i];
     const int col = tk.sh_col[s0 + i];
@@ -126,7 +143,12 @@ __global__ void __launch_bounds__(128) collocation_kernel(ShellsDev sh, TasksDev
     }
     R1 = R1 * V(-2);
     const int64_t o = (int64_t)col * ld + p;
-    eval_shell<GRAD>(sh.l[s], sh.pure[s], dx, dy, dz, R, R1, f + o, fx + o, fy + o, fz + o, ld);
+    if constexpr (MASK) {
+      eval_shell<GRAD>(sh.l[s], sh.pure[s], dx, dy, dz, R, R1, MaxSink{f + o, &mval},
+                       MaxSink{fx + o, &mgrad}, MaxSink{fy + o, &mgrad}, MaxSink{fz + o, &mgrad}, ld);
+    } else {
+      eval_shell<GRAD>(sh.l[s], sh.pure[s], dx, dy, dz, R, R1, f + o, fx + o, fy + o, fz + o, ld);
+    }
   }
   for (int c = tk.nbe[t]; c < tk.nbe_pad[t]; ++c) {
     const int64_t o = (int64_t)c * ld + p;
@@ -136,6 +158,14 @@ __global__ void __launch_bounds__(128) collocation_kernel(ShellsDev sh, TasksDev
       fy[o] = zero;
       fz[o] = zero;
     }
+  }
+  if constexpr (MASK) {
+    // the point's scale sp (power of two above max |phi|) and the key of
+    // max |grad phi|, in the block's FP64 region (PBF64)
+    const PBF64 o(PBDims(np, tk.nbe[t]), GRAD ? 4 : 1);
+    double* base = scr + tk.scr_off[t];
+    base[o.sp + p] = ff::pow2(ff::scale_exponent_f(mval));
+    reinterpret_cast<unsigned*>(base + o.gp)[p] = GRAD ? mgrad : 0u;
   }
 }
 

@@ -71,14 +71,14 @@ def cexpr(e):
 
 def emit(kind, l, polys):
     tag = f"{kind}_{l}"
-    print(f"template <typename T> GB300_HD inline void ang_eval_{tag}"
-          f"(T x, T y, T z, T R, T* __restrict__ out, int64_t s) {{")
+    # O: T* or any type whose operator[] takes a stored value (a value sink)
+    print(f"template <typename T, typename O> GB300_HD inline void ang_eval_{tag}"
+          f"(T x, T y, T z, T R, O out, int64_t s) {{")
     for i, p in enumerate(polys):
         print(f"  out[{i}*s] = R*({cexpr(p)});")
     print("}")
-    print(f"template <typename T> GB300_HD inline void ang_grad_{tag}"
-          f"(T x, T y, T z, T R, T R1, T* __restrict__ f, T* __restrict__ fx,"
-          f" T* __restrict__ fy, T* __restrict__ fz, int64_t s) {{")
+    print(f"template <typename T, typename O> GB300_HD inline void ang_grad_{tag}"
+          f"(T x, T y, T z, T R, T R1, O f, O fx, O fy, O fz, int64_t s) {{")
     for i, p in enumerate(polys):
         dx, dy, dz = sp.diff(p, x), sp.diff(p, y), sp.diff(p, z)
         print(f"  {{ const T S = {cexpr(p)};")

@@ -653,9 +653,8 @@ int64_t DeviceIntegrator::eval_mixed_batches(bool do_vxc) {
       return (int64_t)1;
     });
     launches += timed(5, [&] {
-      launch_point_scales(tk_, mp_, b.b0, b.b1, gga_, f64_, s);
       launch_phi_digits(tk_, mp_, b.b0, b.b1, gga_, f64_, dig_, s);
-      return (int64_t)2;
+      return (int64_t)1;
     });
     launches += timed(6, [&] {
       launch_p_digits(tk_, mp_, b.b0, b.b1, b.max_nu_pad, gga_, P_, prs_, nbf_, f64_, dig_, s);

@@ -525,10 +525,16 @@ __global__ void __launch_bounds__(kThreads, 1)
           // X'[nu, p] = 2^(er + esp - 13) D, a power of two times D
           const int e_row = exp_of_pow2(base[o.r + i]);
           const int e_col = exp_of_pow2(base[o.sp + jc + (lane & 15)]);
-          const float2* ph = reinterpret_cast<const float2*>(base + o.phi2) + i + (int64_t)jc * d.nu128;
+          // phi[q][nu = i][jc .. jc + 15]: 128 contiguous bytes per lane
+          const float4* ph = reinterpret_cast<const float4*>(base + (int64_t)i * d.np + jc);
+          const int64_t qs = o.blk / 2;  // one value plane, in float4
           float2 pf[16];  // phi[nu = i][p] of the pass in hand, float-float
 #pragma unroll
-          for (int n = 0; n < 16; ++n) pf[n] = ph[(int64_t)n * d.nu128];
+          for (int n = 0; n < 8; ++n) {
+            const float4 t = ph[n];
+            pf[2 * n] = make_float2(t.x, t.y);
+            pf[2 * n + 1] = make_float2(t.z, t.w);
+          }
 #pragma unroll
           for (int n = 0; n < 16; ++n) {
             const float sc = ff::pow2f(e_row + __shfl_sync(0xffffffffu, e_col, n) - 13);
@@ -549,7 +555,11 @@ __global__ void __launch_bounds__(kThreads, 1)
             // the next pass's phi values load while this pass is reduced
             if (q + 1 < nq) {
 #pragma unroll
-              for (int n = 0; n < 16; ++n) pf[n] = ph[(q + 1) * o.blk + (int64_t)n * d.nu128];
+              for (int n = 0; n < 8; ++n) {
+                const float4 t = ph[(q + 1) * qs + n];
+                pf[2 * n] = make_float2(t.x, t.y);
+                pf[2 * n + 1] = make_float2(t.z, t.w);
+              }
             }
             reduce16(h, l, lane);
             if ((lane & 1) == 0) {

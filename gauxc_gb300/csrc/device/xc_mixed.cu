@@ -2,7 +2,7 @@
 // (slice) generation for P, phi and Z, and the per-point functional.
 //
 // Layouts per point block (PBDims d: np points, nu basis functions):
-//   FP64 region (at f64_off): PBF64 (phi, scales, phi2)
+//   FP64 region (at f64_off): PBF64 (phi, scales)
 //   digits (bf16, at dig_off): Pd, Fd, Va, Vb in the tiled operand layout of
 //     xc_mixed.cuh (oz_offset); every thread writes 8 consecutive K entries
 //     of one row, i.e. one 16-byte row of a core matrix per digit plane
@@ -59,7 +59,6 @@ struct PBView {
   const ffl* phi;            // [q][mu][p], float-float (collocation of the point blocks)
   double *r, *sp, *cz;
   unsigned* gkey;            // largest |grad phi| of each point, as float magnitude bits
-  float2* phi2;              // [q][p][mu]
   __nv_bfloat16 *Pd, *Fd, *Va, *Vb;
   __device__ PBView(const TasksDev& tk, const MixedPBDev& mp, int b, bool gga, const double* f64c,
                     const __nv_bfloat16* digc)
@@ -70,7 +69,6 @@ struct PBView {
     sp = base + o.sp;
     gkey = reinterpret_cast<unsigned*>(base + o.gp);
     cz = base + o.cz;
-    phi2 = reinterpret_cast<float2*>(base + o.phi2);
     __nv_bfloat16* dg = digc ? const_cast<__nv_bfloat16*>(digc) + mp.dig_off[b] : nullptr;
     Pd = dg + d.pd();
     Fd = dg + d.fd();
@@ -94,30 +92,17 @@ __device__ __forceinline__ unsigned long long row8_max(unsigned long long m,
   return x;
 }
 
-// ---------------------------------------------------------------- point scales
-// sp[p]: power of two above max_mu |phi_mu(p)|; also clears the gradient key.
-__global__ void point_scale_kernel(TasksDev tk, MixedPBDev mp, int b0, double* f64, int gga) {
-  const int b = b0 + blockIdx.y;
-  PBView v(tk, mp, b, gga, f64, nullptr);
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < v.d.np; p += gridDim.x * blockDim.x) {
-    unsigned m = 0;
-    for (int mu = 0; mu < v.d.nu; ++mu) m = max(m, abs_key_f(v.phi[(int64_t)mu * v.d.np + p]));
-    v.sp[p] = ff::pow2(ff::scale_exponent_f(m));
-    v.gkey[p] = 0u;
-  }
-}
-
 // ---------------------------------------------------------------- phi digits
 // Va[mu][p] (K < np) and Vb[mu][np + p] (rows mu < nun): one thread per
-// (mu, 8 points), consecutive threads on consecutive mu.  Fd (rows p, K = mu)
-// and phi2: thread p of the CTA walks the CTA's share of the basis in groups
-// of 8 (kPBMaxPts <= blockDim.x), tracking the point's largest |grad phi|.
+// (mu, 8 points), consecutive threads on consecutive mu.  Fd (rows p, K = mu):
+// thread p of the CTA walks the CTA's share of the basis in groups of 8
+// (kPBMaxPts <= blockDim.x).  The point scales sp come from the collocation
+// kernel.
 __global__ void phi_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const double* f64,
                                   __nv_bfloat16* dig, int gga) {
   const int b = b0 + blockIdx.y;
   PBView v(tk, mp, b, gga, f64, dig);
   const PBDims& d = v.d;
-  const int nq = gga ? 4 : 1;
   const int k2 = 2 * d.np;
   const int stride = gridDim.x * blockDim.x;
   const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
@@ -137,37 +122,24 @@ __global__ void phi_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const doub
     store_digits8(x, es, v.Va + oz_offset(0, mu, p0, kMTile, k2), kMTile * kBK);
     if (mu < d.nun) store_digits8(x, es, v.Vb + oz_offset(0, mu, d.np + p0, kNTile, k2), kNTile * kBK);
   }
-  // transposition: thread (point p, sub-lane sub) takes every nsub-th row
-  // group of this CTA's share, so that small blocks keep all threads busy
+  // Fd: thread (point p, sub-lane sub) takes every nsub-th row group of this
+  // CTA's share, so that small blocks keep all threads busy
   const int nsub = blockDim.x / d.np, sub = threadIdx.x / d.np, p = threadIdx.x % d.np;
   if (sub >= nsub) return;
-  const int ng = d.nu128 / 8;
+  const int ng = d.nu16 / 8;
   const int per = (ng + gridDim.x - 1) / gridDim.x;
   const int g0 = blockIdx.x * per, g1 = min(ng, g0 + per);
-  unsigned gmax = 0;
+  int es[8];
+  const int e0 = exp_of_pow2(v.sp[p]);
+#pragma unroll
+  for (int e = 0; e < 8; ++e) es[e] = e0;
   for (int g = g0 + sub; g < g1; g += nsub) {
     const int mu0 = g * 8;
-    for (int q = 0; q < nq; ++q) {
-      ffl x[8];
+    ffl x[8];
 #pragma unroll
-      for (int e = 0; e < 8; ++e) x[e] = v.phi[q * v.o.blk + (int64_t)(mu0 + e) * d.np + p];
-      float4* dst = reinterpret_cast<float4*>(v.phi2 + q * v.o.blk + (int64_t)p * d.nu128 + mu0);
-#pragma unroll
-      for (int e = 0; e < 4; ++e)
-        dst[e] = make_float4(x[2 * e].hi, x[2 * e].lo, x[2 * e + 1].hi, x[2 * e + 1].lo);
-      if (q == 0 && mu0 < d.nu16) {
-        int es[8];
-        const int e0 = exp_of_pow2(v.sp[p]);
-#pragma unroll
-        for (int e = 0; e < 8; ++e) es[e] = e0;
-        store_digits8(x, es, v.Fd + oz_offset(0, p, mu0, kNTile, d.nu16), kNTile * kBK);
-      }
-      if (q > 0)
-#pragma unroll
-        for (int e = 0; e < 8; ++e) gmax = max(gmax, abs_key_f(x[e]));
-    }
+    for (int e = 0; e < 8; ++e) x[e] = v.phi[(int64_t)(mu0 + e) * d.np + p];
+    store_digits8(x, es, v.Fd + oz_offset(0, p, mu0, kNTile, d.nu16), kNTile * kBK);
   }
-  if (gga && gmax) atomicMax(v.gkey + p, gmax);
 }
 
 // ---------------------------------------------------------------- P digits
@@ -365,13 +337,6 @@ __global__ void functional_kernel(int64_t g0, int64_t g1, const double* __restri
 }
 
 }  // namespace
-
-void launch_point_scales(const TasksDev& tk, const MixedPBDev& mp, int b0, int b1, bool gga,
-                         double* f64, cudaStream_t s) {
-  if (b1 <= b0) return;
-  point_scale_kernel<<<dim3(kPBMaxPts / 128, b1 - b0), 128, 0, s>>>(tk, mp, b0, f64, gga);
-  GB300_CUDA(cudaGetLastError());
-}
 
 void launch_phi_digits(const TasksDev& tk, const MixedPBDev& mp, int b0, int b1, bool gga,
                        const double* f64, __nv_bfloat16* dig, cudaStream_t s) {

@@ -6,12 +6,11 @@
 // kSlices signed digits of 7 bits:  x = 2^e sum_i d_i 2^(-7 i), |d_1| <= 128,
 // |d_i| <= 64 (i > 1).  Digit i is stored in BF16 as d_i 2^(-7 (i - 1)), which
 // is exact.  A product is the sum over slice pairs (i, j) with i + j <= kLevels
-// of BF16 GEMMs; pairs of equal i + j share one TMEM accumulator, so each of
-// the three leading levels is an exact integer sum in FP32 (the K extent of
-// one GEMM is at most 512: 512 * 3 * 2^13 < 2^24).  The remaining pairs
-// (relative weight 2^-21 and below) share a fourth accumulator, whose FP32
-// rounding stays below 2^-44 of the result.  The epilogue adds the levels in
-// float-float arithmetic.
+// of BF16 GEMMs (21 pairs); pairs of equal i + j share one TMEM accumulator,
+// each an exact integer sum in FP32 (the K extent of one GEMM is at most 512:
+// 512 * 3 * 2^13 < 2^24).  The epilogue adds the six levels in float-float
+// arithmetic (the three smallest, 2^-21 of the result and below, first in
+// FP32).
 //
 // GEMM operands live in HBM already in the tensor core's shared-memory image:
 // tiles of TR rows (128 for the M operand, 64 for the N operand) by kBK
@@ -70,13 +69,14 @@ struct PBDims {
 // FP64 region of a point block (offsets in doubles): phi[q][mu][p] (q = value,
 // d/dx, d/dy, d/dz; nu128 rows), r[nu128] (row scales of P), sp[np] (point
 // scales of phi), gp[np] (largest |grad phi| of a point, as an IEEE magnitude
-// key), cz[nu128] (scale of Z, one value per block), then phi2[q][p][mu], the
-// values of phi transposed as float-float pairs (one double's worth each).
+// key), cz[nu128] (scale of Z, one value per block).  phi entries are
+// float-float pairs (one double's worth each); sp and gp are written by the
+// collocation kernel.
 struct PBF64 {
-  int64_t blk, r, sp, gp, cz, phi2, total;
+  int64_t blk, r, sp, gp, cz, total;
   __host__ __device__ PBF64(const PBDims& d, int nq)
       : blk((int64_t)d.np * d.nu128), r(nq * blk), sp(r + d.nu128), gp(sp + d.np),
-        cz(gp + d.np), phi2(cz + d.nu128), total(phi2 + nq * blk) {}
+        cz(gp + d.np), total(cz + d.nu128) {}
 };
 
 // Point blocks (merged tasks of one atom) reuse TasksDev (npts_pad = np,
@@ -130,8 +130,6 @@ void launch_collocation_masked(const ShellsDev& sh, const TasksDev& tk, const PB
                                cudaStream_t s);
 
 // Digits / scales.  All launchers take the batch's point-block range [b0, b1).
-void launch_point_scales(const TasksDev& tk, const MixedPBDev& mp, int b0, int b1, bool gga,
-                         double* f64, cudaStream_t s);
 void launch_phi_digits(const TasksDev& tk, const MixedPBDev& mp, int b0, int b1, bool gga,
                        const double* f64, __nv_bfloat16* dig, cudaStream_t s);
 // rs[i]: power of two above max_j |P[i][j]| (launch_p_row_scales, once per call)
