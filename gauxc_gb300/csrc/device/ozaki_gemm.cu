@@ -80,7 +80,7 @@ constexpr int kWorkWarps = kEpiWarps - 2;  // draining warps that also process (
 constexpr int kRedOffset = kStages * kStageBytes;  // per working warp: parked chunk / transposition
 constexpr int kHandOffset = kRedOffset + kWorkWarps * kChunkBytes;
 constexpr int kBarOffset = kHandOffset + 4 * kChunkBytes;  // the four quarter-1 chunks
-constexpr uint32_t kWaitLimit = 1u << 22;
+constexpr uint64_t kWaitLimit = 1000000000ull;  // ns a pipeline wait may take before it counts as failed
 constexpr uint16_t kClusterMask = (1u << kCluster) - 1;
 static_assert(kBK == 16, "one MMA (K = 16) per operand tile");
 static_assert(kABytes % (16 * 12) == 0, "A shares of 1/2, 1/3, 1/4 are 16-byte multiples");
@@ -286,6 +286,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 
   if (warp == 0) {
     // ------------------------------------------------------------ producer
+    const uint64_t pol = umma::l2_evict_first_policy();
     uint32_t g = 0;
     SlotItems cur, nxt;
     if (beg < end) load_slot(sched.items, beg, cur);
@@ -314,11 +315,22 @@ __global__ void __launch_bounds__(kThreads, 1)
             umma::mbar_arrive_expect_tx(&B->full[st], kStageBytes);
             uint8_t* sa = smem + st * kStageBytes;
             const uint8_t* ga = A + (int64_t)u * kABytes;
-            if (v.nparts > 1)
-              umma::bulk_g2s_multicast(sa + a_lo, ga + a_lo, a_hi - a_lo, &B->full[st], v.mask);
-            else
-              umma::bulk_g2s(sa, ga, kABytes, &B->full[st]);
-            umma::bulk_g2s(sa + kABytes, Bm + (int64_t)u * kBBytes, kBBytes, &B->full[st]);
+            if (EPI == EPI_V) {
+              // operands leave L2 before the lines of the VXC accumulator
+              // that the epilogue's atomics keep updating
+              if (v.nparts > 1)
+                umma::bulk_g2s_multicast_hint(sa + a_lo, ga + a_lo, a_hi - a_lo, &B->full[st],
+                                              v.mask, pol);
+              else
+                umma::bulk_g2s_hint(sa, ga, kABytes, &B->full[st], pol);
+              umma::bulk_g2s_hint(sa + kABytes, Bm + (int64_t)u * kBBytes, kBBytes, &B->full[st], pol);
+            } else {
+              if (v.nparts > 1)
+                umma::bulk_g2s_multicast(sa + a_lo, ga + a_lo, a_hi - a_lo, &B->full[st], v.mask);
+              else
+                umma::bulk_g2s(sa, ga, kABytes, &B->full[st]);
+              umma::bulk_g2s(sa + kABytes, Bm + (int64_t)u * kBBytes, kBBytes, &B->full[st]);
+            }
           } else {
             umma::mbar_arrive(&B->full[st]);  // no tile (or a shorter one): empty use
           }
