@@ -152,16 +152,18 @@ def setup_workload(cfg_idx, lwd):
 
 
 def pinned_like(P):
-    """Pinned host buffers when torch is present (pageable numpy otherwise)."""
+    """Host P / VXC buffers page-locked in place through the library (what an
+    SCF code does with the buffers it passes every iteration)."""
+    import gauxc_gb300 as g
+    a = np.asfortranarray(P).copy(order="F")
+    v = np.zeros_like(a, order="F")
     try:
-        import torch
-        tP = torch.empty(P.shape[::-1], dtype=torch.float64).pin_memory()
-        a = tP.numpy().T  # Fortran-ordered view
-        a[...] = P
-        tV = torch.empty(P.shape[::-1], dtype=torch.float64).pin_memory()
-        return a, tV.numpy().T, True, (tP, tV)
+        g.host_register(a)
+        g.host_register(v)
+        pinned = True
     except Exception:
-        return np.asfortranarray(P), np.zeros_like(P, order="F"), False, None
+        pinned = False
+    return a, v, pinned, (a, v)
 
 
 def eval_into(integ, P, V):
@@ -431,7 +433,7 @@ def main():
     barrier(dist)
     sampler.start()
     comp, wall, launches = [], [], 0
-    kt = {}
+    kt, brk = {}, {}
     t_all0 = time.perf_counter()
     for _ in range(args.steps):
         t0 = time.perf_counter()
@@ -439,6 +441,8 @@ def main():
         wall.append(time.perf_counter() - t0)
         tm = integ.timings()
         comp.append(tm["compute_ms"] * 1e-3)
+        for k in ("h2d_ms", "compute_ms", "d2h_ms", "wall_ms"):
+            brk.setdefault(k, []).append(tm.get(k, 0.0))
         st = integ.plan_stats()
         launches += int(st["gpu_launches"])
         for k, v in integ.kernel_times().items():
@@ -532,7 +536,8 @@ def main():
                     l2="inputs larger than L2 (scratch %.1f GB per batch)" % (stats["scratch_bytes"] / 1e9),
                     parallelism=f"replicas x{args.gpus}"),
         e2e=dict(value=e2e, unit="s", h2d_bytes_per_step=nbf * nbf * 8,
-                 d2h_bytes_per_step=nbf * nbf * 8 + 16, pinned=pinned),
+                 d2h_bytes_per_step=nbf * nbf * 8 + 16, pinned=pinned,
+                 breakdown_ms={k: float(np.mean(v)) for k, v in brk.items()}),
         roofline=roofline, cpu_baseline=cpu, gpu_launches=launches, clocks=clocks,
         fp64_check=fp64_check,
         exc=exc, nel=integ.last_nel(),

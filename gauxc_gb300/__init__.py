@@ -27,7 +27,8 @@ __all__ = [
     "MolecularWeightsSettings", "MolecularWeights", "MolecularWeightsFactory",
     "functional_type", "XCIntegrator", "XCIntegratorFactory", "IntegratorBatch", "lib",
     "device_count",
-    "ssf_weights", "collocation", "set_device", "measure_fp64_peak",
+    "ssf_weights", "collocation", "set_device", "measure_fp64_peak", "host_register",
+    "host_unregister",
 ]
 
 class _LazyLibrary:
@@ -61,6 +62,18 @@ def set_device(dev):
 def tensor_core_selftest(n=256, k=256):
     """Worst relative error of the tensor-core emulated-FP64 GEMM on random data."""
     return float(_call(_L.gauxc_gb300_tensor_core_selftest, int(n), int(k)))
+
+
+def host_register(a):
+    """Page-locks the memory of numpy array `a` in place (for P / VXC buffers
+    reused every SCF iteration); True when it registered it."""
+    return bool(_call(_L.gauxc_gb300_host_register, ctypes.c_void_p(a.ctypes.data),
+                      ctypes.c_size_t(a.nbytes)))
+
+
+def host_unregister(a):
+    """Undoes host_register."""
+    _call(_L.gauxc_gb300_host_unregister, ctypes.c_void_p(a.ctypes.data))
 
 
 def measure_fp64_peak():

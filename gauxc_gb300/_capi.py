@@ -124,6 +124,8 @@ PROTOTYPES = {
     "gauxc_gb300_integrator_set_profiling": (None, [S, GauXCIntegrator, b]),
     "gauxc_gb300_integrator_kernel_times": (I, [S, GauXCIntegrator, P(dbl), I]),
     "gauxc_gb300_measure_fp64_peak": (dbl, [S]),
+    "gauxc_gb300_host_register": (ctypes.c_int, [S, ctypes.c_void_p, ctypes.c_size_t]),
+    "gauxc_gb300_host_unregister": (None, [S, ctypes.c_void_p]),
     "gauxc_gb300_set_device": (None, [S, I]),
     "gauxc_gb300_tensor_core_selftest": (dbl, [S, I, I]),
     "gauxc_gb300_ssf_weights": (None, [S, i64, i32, P(dbl), P(i32), P(dbl), P(dbl), P(dbl)]),

@@ -59,6 +59,22 @@ double measure_fp64_peak() {
 
 void set_device(int d) { GB300_CUDA(cudaSetDevice(d)); }
 
+bool host_register(void* p, size_t bytes) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) == cudaSuccess && a.type != cudaMemoryTypeUnregistered)
+    return false;
+  cudaGetLastError();
+  const cudaError_t e = cudaHostRegister(p, bytes, cudaHostRegisterDefault);
+  if (e == cudaErrorHostMemoryAlreadyRegistered) {
+    cudaGetLastError();
+    return false;
+  }
+  GB300_CUDA(e);
+  return true;
+}
+
+void host_unregister(void* p) { GB300_CUDA(cudaHostUnregister(p)); }
+
 double tensor_core_selftest(int n, int k) {
   if (cuda_device_count() == 0) throw error("no CUDA device available");
   return ozaki_selftest(n, k);

@@ -815,6 +815,18 @@ void gauxc_gb300_batch_delete(GauXCStatus* status, GauXCGB300Batch* batch) {
   destroy<BatchHandle>(batch);
 }
 
+int gauxc_gb300_host_register(GauXCStatus* status, void* ptr, size_t bytes) {
+  status_init(status);
+  int r = 0;
+  guarded(status, [&] { r = host_register(ptr, bytes) ? 1 : 0; });
+  return r;
+}
+
+void gauxc_gb300_host_unregister(GauXCStatus* status, void* ptr) {
+  status_init(status);
+  guarded(status, [&] { host_unregister(ptr); });
+}
+
 double gauxc_gb300_measure_fp64_peak(GauXCStatus* status) {
   status_init(status);
   double r = 0.;

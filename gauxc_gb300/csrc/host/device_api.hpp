@@ -84,6 +84,10 @@ std::map<std::string, double> batch_timings(const IntegratorBatch& b);
 
 // FP64 FMA throughput probe (TFLOP/s) on the current device.
 double measure_fp64_peak();
+// Page-locks caller host memory in place (cudaHostRegister); false when it
+// already is page-locked (nothing done).  host_unregister undoes it.
+bool host_register(void* p, size_t bytes);
+void host_unregister(void* p);
 // Tensor-core emulated-FP64 GEMM self-test: worst relative error.
 double tensor_core_selftest(int n, int k);
 void set_device(int dev);

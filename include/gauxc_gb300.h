@@ -270,6 +270,12 @@ int gauxc_gb300_integrator_kernel_times(GauXCStatus* status, const GauXCIntegrat
                                         double* out, int nmax);
 /* Measured FP64 FMA throughput of the current device in TFLOP/s (about 50 ms probe). */
 double gauxc_gb300_measure_fp64_peak(GauXCStatus* status);
+/* Page-lock caller host memory in place (P / VXC buffers reused every SCF
+   iteration) so that the copies of eval_* run at page-locked bandwidth.
+   Returns 1 when it registered the range, 0 when it already was page-locked.
+   The memory must stay allocated until gauxc_gb300_host_unregister. */
+int gauxc_gb300_host_register(GauXCStatus* status, void* ptr, size_t bytes);
+void gauxc_gb300_host_unregister(GauXCStatus* status, void* ptr);
 /* Self-test of the tensor-core (split-mantissa BF16) VXC GEMM: the symmetric
    n x n product F Z^T + Z F^T over k points (n multiple of 128, k multiple of
    64, k <= 256) against FP64; returns the worst error relative to the largest
