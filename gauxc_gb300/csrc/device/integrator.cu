@@ -688,8 +688,12 @@ int64_t DeviceIntegrator::enqueue(const double* P, int64_t ldp, double* VXC, int
   cudaStream_t s = stream_;
   const size_t row = (size_t)nbf_ * sizeof(double);
   if (events) GB300_CUDA(cudaEventRecord(ev_[0], s));
-  GB300_CUDA(cudaMemcpy2DAsync(P_, row, P, (size_t)ldp * sizeof(double), row, nbf_,
-                               cudaMemcpyHostToDevice, s));
+  // one linear copy when P is contiguous (a pitched copy moves row by row)
+  if (ldp == nbf_)
+    GB300_CUDA(cudaMemcpyAsync(P_, P, row * nbf_, cudaMemcpyHostToDevice, s));
+  else
+    GB300_CUDA(cudaMemcpy2DAsync(P_, row, P, (size_t)ldp * sizeof(double), row, nbf_,
+                                 cudaMemcpyHostToDevice, s));
   if (events) GB300_CUDA(cudaEventRecord(ev_[1], s));
   if (do_vxc) GB300_CUDA(cudaMemsetAsync(A_, 0, (size_t)nbf_ * nbf_ * sizeof(double), s));
   int64_t launches = 0;
@@ -729,9 +733,13 @@ int64_t DeviceIntegrator::enqueue(const double* P, int64_t ldp, double* VXC, int
     return (int64_t)1;
   });
   if (events) GB300_CUDA(cudaEventRecord(ev_[2], s));
-  if (do_vxc)
-    GB300_CUDA(cudaMemcpy2DAsync(VXC, (size_t)ldvxc * sizeof(double), V_, row, row, nbf_,
-                                 cudaMemcpyDeviceToHost, s));
+  if (do_vxc) {
+    if (ldvxc == nbf_)
+      GB300_CUDA(cudaMemcpyAsync(VXC, V_, row * nbf_, cudaMemcpyDeviceToHost, s));
+    else
+      GB300_CUDA(cudaMemcpy2DAsync(VXC, (size_t)ldvxc * sizeof(double), V_, row, row, nbf_,
+                                   cudaMemcpyDeviceToHost, s));
+  }
   GB300_CUDA(cudaMemcpyAsync(en_host, out_, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
   GB300_CUDA(cudaMemcpyAsync(err_host, err_, sizeof(int), cudaMemcpyDeviceToHost, s));
   if (events) GB300_CUDA(cudaEventRecord(ev_[3], s));

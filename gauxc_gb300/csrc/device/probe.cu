@@ -60,10 +60,6 @@ double measure_fp64_peak() {
 void set_device(int d) { GB300_CUDA(cudaSetDevice(d)); }
 
 bool host_register(void* p, size_t bytes) {
-  cudaPointerAttributes a{};
-  if (cudaPointerGetAttributes(&a, p) == cudaSuccess && a.type != cudaMemoryTypeUnregistered)
-    return false;
-  cudaGetLastError();
   const cudaError_t e = cudaHostRegister(p, bytes, cudaHostRegisterDefault);
   if (e == cudaErrorHostMemoryAlreadyRegistered) {
     cudaGetLastError();
