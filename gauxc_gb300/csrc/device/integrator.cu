@@ -105,6 +105,14 @@ class DeviceIntegrator {
       : func_(f), prec_(prec), params_(pp), arena_(&rt), rt_(&rt) {
     if (cuda_device_count() == 0) throw error("no CUDA device available for the device integrator");
     GB300_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    {
+      // the device can address pageable host memory (coherent host link):
+      // P and VXC move by kernels reading / writing the caller's buffers
+      int dev = 0, pma = 0;
+      GB300_CUDA(cudaGetDevice(&dev));
+      GB300_CUDA(cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, dev));
+      host_direct_ = pma != 0;
+    }
     for (auto& e : ev_) GB300_CUDA(cudaEventCreate(&e));
     build(lb);
   }
@@ -160,6 +168,7 @@ class DeviceIntegrator {
   double* scr_ = nullptr;
   double4* zcoef_ = nullptr;
   double2* partials_ = nullptr;
+  bool host_direct_ = false;  // P / VXC moved by kernels (pageable memory access)
   double* P_ = nullptr;
   double* A_ = nullptr;
   double* V_ = nullptr;
@@ -231,7 +240,7 @@ void DeviceIntegrator::build(const LoadBalancer& lb) {
 
   P_ = arena_.alloc<double>((size_t)nbf_ * nbf_);
   A_ = arena_.alloc<double>((size_t)nbf_ * nbf_);
-  V_ = arena_.alloc<double>((size_t)nbf_ * nbf_);
+  if (!host_direct_) V_ = arena_.alloc<double>((size_t)nbf_ * nbf_);  // staging for the copy out
   out_ = arena_.alloc<double>(2);
   err_ = arena_.alloc<int>(1);
   GB300_CUDA(cudaMemsetAsync(err_, 0, sizeof(int), s));
@@ -688,15 +697,18 @@ int64_t DeviceIntegrator::enqueue(const double* P, int64_t ldp, double* VXC, int
   cudaStream_t s = stream_;
   const size_t row = (size_t)nbf_ * sizeof(double);
   if (events) GB300_CUDA(cudaEventRecord(ev_[0], s));
-  // one linear copy when P is contiguous (a pitched copy moves row by row)
-  if (ldp == nbf_)
+  if (host_direct_) {
+    // the device reads the caller's (pageable or page-locked) P itself
+    launch_copy_matrix(P, ldp, P_, nbf_, nbf_, s);
+  } else if (ldp == nbf_) {
     GB300_CUDA(cudaMemcpyAsync(P_, P, row * nbf_, cudaMemcpyHostToDevice, s));
-  else
+  } else {
     GB300_CUDA(cudaMemcpy2DAsync(P_, row, P, (size_t)ldp * sizeof(double), row, nbf_,
                                  cudaMemcpyHostToDevice, s));
+  }
   if (events) GB300_CUDA(cudaEventRecord(ev_[1], s));
+  int64_t launches = host_direct_ ? 1 : 0;
   if (do_vxc) GB300_CUDA(cudaMemsetAsync(A_, 0, (size_t)nbf_ * nbf_ * sizeof(double), s));
-  int64_t launches = 0;
   pev_used_ = 0;
   if (prec_ == Precision::Mixed) launches += eval_mixed_batches(do_vxc);
   for (const Batch& b : batches_) {
@@ -723,7 +735,7 @@ int64_t DeviceIntegrator::enqueue(const double* P, int64_t ldp, double* VXC, int
       });
     }
   }
-  if (do_vxc)
+  if (do_vxc && !host_direct_)
     launches += timed(4, [&] {
       launch_symmetrize(A_, nbf_, V_, nbf_, s);
       return (int64_t)1;
@@ -734,11 +746,16 @@ int64_t DeviceIntegrator::enqueue(const double* P, int64_t ldp, double* VXC, int
   });
   if (events) GB300_CUDA(cudaEventRecord(ev_[2], s));
   if (do_vxc) {
-    if (ldvxc == nbf_)
+    if (host_direct_) {
+      // VXC = A + A^T written straight into the caller's buffer
+      launch_symmetrize(A_, nbf_, VXC, ldvxc, s);
+      ++launches;
+    } else if (ldvxc == nbf_) {
       GB300_CUDA(cudaMemcpyAsync(VXC, V_, row * nbf_, cudaMemcpyDeviceToHost, s));
-    else
+    } else {
       GB300_CUDA(cudaMemcpy2DAsync(VXC, (size_t)ldvxc * sizeof(double), V_, row, row, nbf_,
                                    cudaMemcpyDeviceToHost, s));
+    }
   }
   GB300_CUDA(cudaMemcpyAsync(en_host, out_, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
   GB300_CUDA(cudaMemcpyAsync(err_host, err_, sizeof(int), cudaMemcpyDeviceToHost, s));

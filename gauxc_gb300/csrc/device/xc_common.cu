@@ -73,6 +73,26 @@ void launch_symmetrize(const double* A, int nbf, double* vxc, int64_t ld, cudaSt
   GB300_CUDA(cudaGetLastError());
 }
 
+// dst(:, c) = src(:, c) for the n x n column-major matrices (leading
+// dimensions lds, ldd); either side may be host memory the device can
+// address (pageable memory access).
+__global__ void copy_matrix_kernel(const double* __restrict__ src, int64_t lds,
+                                   double* __restrict__ dst, int64_t ldd, int n) {
+  const int64_t total = (int64_t)n * n;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = i / n, r = i - c * n;
+    dst[c * ldd + r] = src[c * lds + r];
+  }
+}
+
+void launch_copy_matrix(const double* src, int64_t lds, double* dst, int64_t ldd, int n,
+                        cudaStream_t s) {
+  if (n <= 0) return;
+  copy_matrix_kernel<<<1216, 256, 0, s>>>(src, lds, dst, ldd, n);
+  GB300_CUDA(cudaGetLastError());
+}
+
 void launch_reduce_partials(const double2* partials, int64_t n, double* out, cudaStream_t s) {
   reduce_partials_kernel<<<1, 256, 0, s>>>(partials, n, out);
   GB300_CUDA(cudaGetLastError());

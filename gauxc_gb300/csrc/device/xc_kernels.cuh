@@ -15,6 +15,9 @@ void launch_vxc_fp64(const TasksDev& tk, const int4* items, int nitems, const do
 
 // VXC(i,j) = A(i,j) + A(j,i), written with leading dimension ld.
 void launch_symmetrize(const double* A, int nbf, double* vxc, int64_t ld, cudaStream_t s);
+// dst = src for n x n column-major matrices; either may be device-addressable host memory.
+void launch_copy_matrix(const double* src, int64_t lds, double* dst, int64_t ldd, int n,
+                        cudaStream_t s);
 // out[0] = sum of partials[i].x, out[1] = sum of partials[i].y (compensated,
 // fixed order, single CTA)
 void launch_reduce_partials(const double2* partials, int64_t n, double* out, cudaStream_t s);

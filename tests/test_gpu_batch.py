@@ -102,3 +102,17 @@ def test_plan_params_validated(g, members):
     r["imx"].set_plan_params(pb_max_pts=128, nu2_weight=100.0)
     e, v = r["imx"].eval_exc_vxc(r["P"])
     assert abs(e - r["e64"]) <= TOL_MIXED
+
+
+def test_host_register_keeps_results(g, members):
+    """P page-locked in place through the library gives the same results."""
+    r = members[1]
+    P = np.asfortranarray(r["P"].copy())
+    g.host_register(P)
+    try:
+        assert g.host_register(P) is False  # already page-locked
+        e, v = r["i64"].eval_exc_vxc(P)
+    finally:
+        g.host_unregister(P)
+    assert abs(e - r["e64"]) <= TOL_SAME
+    assert np.abs(v - r["v64"]).max() <= TOL_SAME
