@@ -13,8 +13,11 @@
 #include "core.hpp"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <exception>
 #include <limits>
+#include <thread>
 
 namespace gb300 {
 
@@ -47,8 +50,11 @@ std::shared_ptr<LoadBalancer> make_load_balancer(std::shared_ptr<const Molecule>
   lb->meta = std::make_shared<MolMeta>(*mol);
   lb->device_screening = device;
 
-  std::vector<XCTask> tasks;
-  for (size_t iat = 0; iat < mol->size(); ++iat) {
+  // Task candidates of every atom, atoms spread over host threads; the lists
+  // are joined in atom order, so the result does not depend on the threads.
+  const size_t nat = mol->size();
+  std::vector<std::vector<XCTask>> per_atom(nat);
+  auto atom_tasks = [&](size_t iat) {
     const Atom& at = (*mol)[iat];
     const double c[3] = {at.x, at.y, at.z};
     const AtomicGrid& g = mg->grids.at(at.Z);
@@ -76,9 +82,32 @@ std::shared_ptr<LoadBalancer> make_load_balancer(std::shared_ptr<const Molecule>
       t.shell_list = screen_box(*basis, lo, up, t.nbe);
       if (t.shell_list.empty()) continue;
       t.dist_nearest = lb->meta->dist_nearest[iat];
-      tasks.push_back(std::move(t));
+      per_atom[iat].push_back(std::move(t));
     }
+  };
+  {
+    const size_t nth = std::min<size_t>(nat, std::max(1u, std::thread::hardware_concurrency()));
+    std::atomic<size_t> next{0};
+    std::exception_ptr failure;
+    std::atomic<bool> failed{false};
+    auto worker = [&]() {
+      for (size_t i; !failed && (i = next++) < nat;) {
+        try {
+          atom_tasks(i);
+        } catch (...) {
+          if (!failed.exchange(true)) failure = std::current_exception();
+        }
+      }
+    };
+    std::vector<std::thread> pool;
+    for (size_t k = 1; k < nth; ++k) pool.emplace_back(worker);
+    worker();
+    for (auto& th : pool) th.join();
+    if (failure) std::rethrow_exception(failure);
   }
+  std::vector<XCTask> tasks;
+  for (auto& v : per_atom)
+    for (auto& t : v) tasks.push_back(std::move(t));
 
   std::stable_sort(tasks.begin(), tasks.end(), [](const XCTask& a, const XCTask& b) {
     if (a.iParent != b.iParent) return a.iParent < b.iParent;
