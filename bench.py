@@ -365,6 +365,9 @@ def main():
     args = ap.parse_args()
     ws, rank, local = dist_env()
     dist = init_dist(ws)
+    if ws > 1:
+        # cluster multicast of GEMM operands only in single-GPU runs
+        os.environ.setdefault("GAUXC_GB300_CLUSTER_MULTICAST", "0")
 
     import gauxc_gb300 as g
     from gauxc_gb300 import workloads as W

@@ -112,6 +112,8 @@ class DeviceIntegrator {
       GB300_CUDA(cudaGetDevice(&dev));
       GB300_CUDA(cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, dev));
       host_direct_ = pma != 0;
+      const char* mc = std::getenv("GAUXC_GB300_CLUSTER_MULTICAST");
+      multicast_ = (mc && std::string(mc) == "0") ? 0 : 1;
     }
     for (auto& e : ev_) GB300_CUDA(cudaEventCreate(&e));
     build(lb);
@@ -169,6 +171,9 @@ class DeviceIntegrator {
   double4* zcoef_ = nullptr;
   double2* partials_ = nullptr;
   bool host_direct_ = false;  // P / VXC moved by kernels (pageable memory access)
+  // A-operand multicast inside GEMM clusters; GAUXC_GB300_CLUSTER_MULTICAST=0
+  // turns it off (processes that share a run with other GPUs)
+  int multicast_ = 1;
   double* P_ = nullptr;
   double* A_ = nullptr;
   double* V_ = nullptr;
@@ -670,7 +675,7 @@ int64_t DeviceIntegrator::eval_mixed_batches(bool do_vxc) {
       return (int64_t)1;
     });
     launches += timed(1, [&] {
-      launch_ozaki_x(tk_, mp_, OzSchedule{slots_, sched_ + b.x_sched, b.x_ncl}, f64_, dig_, gga_,
+      launch_ozaki_x(tk_, mp_, OzSchedule{slots_, sched_ + b.x_sched, b.x_ncl, multicast_}, f64_, dig_, gga_,
                      rho4_, err_, s);
       return (int64_t)1;
     });
@@ -684,7 +689,7 @@ int64_t DeviceIntegrator::eval_mixed_batches(bool do_vxc) {
       return (int64_t)2;
     });
     launches += timed(3, [&] {
-      launch_ozaki_v(tk_, mp_, OzSchedule{slots_, sched_ + b.v_sched, b.v_ncl}, f64_, dig_, gga_,
+      launch_ozaki_v(tk_, mp_, OzSchedule{slots_, sched_ + b.v_sched, b.v_ncl, multicast_}, f64_, dig_, gga_,
                      A_, nbf_, err_, s);
       return (int64_t)1;
     });

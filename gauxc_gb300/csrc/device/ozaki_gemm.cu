@@ -229,7 +229,7 @@ __device__ __forceinline__ bool same_a(const OzItem& a, const OzItem& b) {
   return a.pb == b.pb && a.m0 == b.m0 && a.k0 == b.k0 && a.k1 == b.k1;
 }
 
-__device__ __forceinline__ SlotView view_of(const SlotItems& s, int rank) {
+__device__ __forceinline__ SlotView view_of(const SlotItems& s, int rank, bool multicast) {
   SlotView v;
 #pragma unroll
   for (int r = 0; r < kCluster; ++r)
@@ -241,7 +241,8 @@ __device__ __forceinline__ SlotView view_of(const SlotItems& s, int rank) {
   for (int r = 0; r < kCluster; ++r) {
     if (s.q[r].pb < 0) continue;
     v.uses = max(v.uses, (s.q[r].k1 - s.q[r].k0) / kBK);
-    if (v.it.pb >= 0 && same_a(s.q[r], v.it)) v.mask |= (uint16_t)(1u << r);
+    if (v.it.pb >= 0 && (multicast || r == rank) && same_a(s.q[r], v.it))
+      v.mask |= (uint16_t)(1u << r);
   }
   v.part = __popc(v.mask & ((1u << rank) - 1));
   v.nparts = __popc(v.mask);
@@ -295,7 +296,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (warp_failed(B)) break;
       // the next slot's entries load while this slot's copies are issued
       if (sl + 1 < end) load_slot(sched.items, sl + 1, nxt);
-      const SlotView v = view_of(cur, rank);
+      const SlotView v = view_of(cur, rank, sched.multicast != 0);
       const uint8_t* A = reinterpret_cast<const uint8_t*>(dig + v.it.a);
       const uint8_t* Bm = reinterpret_cast<const uint8_t*>(dig + v.it.b);
       const uint32_t a_lo = (uint32_t)(v.part * kABytes / max(v.nparts, 1));
@@ -358,7 +359,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int sl = beg; sl < end; ++sl) {
       if (warp_failed(B)) break;
       if (sl + 1 < end) load_slot(sched.items, sl + 1, nxt);
-      const SlotView v = view_of(cur, rank);
+      const SlotView v = view_of(cur, rank, sched.multicast != 0);
       // the epilogue has drained the previous tile's accumulators
       if (v.nkb > 0 && li >= 1 && !warp_wait(&B->tempty, (li - 1) & 1)) {
         if (lane == 0) set_fail(B, ERR_TEMPTY);

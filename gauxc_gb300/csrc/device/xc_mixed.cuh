@@ -118,11 +118,13 @@ inline void oz_set_operands(OzItem& it, const PBDims& d, int64_t dig_off, bool v
 // Work list of one persistent GEMM launch on clusters of kCluster CTAs:
 // cluster c processes slots slot_off[c] .. slot_off[c + 1] - 1 in order; CTA
 // r of the cluster takes items[kCluster * slot + r] (pb < 0: none).
+// multicast = 0: every CTA loads its own A operand (no cluster multicast).
 constexpr int kCluster = 4;
 struct OzSchedule {
   const OzItem* items;
   const int* slot_off;
   int nclusters;
+  int multicast = 1;
 };
 
 void launch_collocation_masked(const ShellsDev& sh, const TasksDev& tk, const PBMaskDev& mk,
