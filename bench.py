@@ -1,12 +1,15 @@
-"""EXC+VXC time per SCF iteration on one GB300 (replicas across GPUs).
+"""EXC+VXC time per SCF iteration on one GB300.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+  python bench.py [--steps K] [--warmup W] [--impl gb300|reference]
                   [--config IDX] [--lwd Default|GB300-FP64|GB300-Mixed]
 
 Default: workload 4 (256 waters, PBE, 15360 bf) on the tensor-core path
 ("GB300-Mixed"), with the plain FP64 device path run once beside it for the
 speed-up and the |dEXC| / max|dVXC| check.  Workload 3 is the batched case
 (64 clusters, every SCF iteration one CUDA-graph launch).
+
+The integrator runs on one GPU: with --gpus N > 1 (or WORLD_SIZE > 1) this
+arm prints one "unavailable" line and exits 0.
 
 A step is one eval_exc_vxc(P) call of the workload: the device-resident plan
 (tasks, SSF weights, maps) is built during the untimed warm-up; each timed
@@ -16,12 +19,15 @@ call copies P in, runs the whole XC pass and copies VXC out.
   e2e    -- wall time of the public C-ABI call with pinned host P / VXC
             (host->device copy, XC pass, device->host copy, synchronize)
 --impl reference times the CPU restatement of the reference host integrator
-(oracle/, OpenMP, all host cores) on a bounded sample of the same tasks and
-extrapolates to one full iteration by the sample's share of sum npts*nbe^2.
+(oracle/: per-task collocation, BLAS dgemm / dsyr2k contractions as in the
+reference host driver, OpenMP over tasks on all host cores) on a fixed
+strided sample of the same tasks, extrapolated to one full iteration by the
+sample's share of sum npts*nbe^2 (the contractions' work).
 """
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -33,7 +39,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "EXC+VXC time/SCF iter on 1 GB300: mixed-prec batched vs FP64 GPU at |\u0394EXC|\u22641e-8 Eh"
+METRIC = "EXC+VXC time/SCF iter on 1 GB300: mixed-prec batched vs FP64 GPU at |ΔEXC|≤1e-8 Eh"
 WORKLOADS = {
     0: "1 water, SVWN5, MK 75x302 unpruned, 60 bf",
     1: "32 waters (10 A cube), PBE, MK 99x590 Treutler, 1920 bf, nocc 160",
@@ -43,6 +49,9 @@ WORKLOADS = {
     4: "256 waters (20 A cube), PBE, MK 75x302 Treutler, tol 1e-12, 15360 bf, nocc 1280",
     5: "profiling case: 4 waters (6 A cube), PBE, MK 99x590 Treutler, 240 bf",
 }
+# Slice-pair products per emulated FP64 product (6 digits, levels i + j <= 5).
+SLICE_PAIRS = 21
+KCLASSES = ["collocation", "density", "zmat", "vxc", "other", "phi_digits", "p_digits"]
 
 
 class ClockSampler:
@@ -101,37 +110,81 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+def cpu_model():
+    """CPU model name and core count of this host."""
+    name = None
+    try:
+        out = subprocess.run(["lscpu"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                             text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.lower().startswith("model name"):
+                name = ln.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if not name:
+        try:
+            for ln in open("/proc/cpuinfo"):
+                if ln.lower().startswith(("model name", "cpu model")):
+                    name = ln.split(":", 1)[1].strip()
+                    break
+        except OSError:
+            pass
+    return f"{name or platform.processor() or platform.machine()} ({platform.machine()})"
 
 
-def init_dist(ws):
-    if ws <= 1:
-        return None
-    import torch.distributed as dist
-    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
-    dist.init_process_group("gloo")
-    return dist
+def peaks():
+    pp = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pp):
+        try:
+            return json.load(open(pp)), "MEASURED_PEAKS.json"
+        except (ValueError, OSError):
+            pass
+    return {}, None
 
 
-def reduce_max(dist, x):
-    if dist is None:
-        return x
-    import torch
-    t = torch.tensor([float(x)], dtype=torch.float64)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+def tensor_peak():
+    pk, src = peaks()
+    if pk.get("bf16_tflops_sustained"):
+        return float(pk["bf16_tflops_sustained"]), "bf16_tflops_sustained (of measured)"
+    return 1700.0, "sustained bf16 1.7 PFLOP/s (of fallback)"
 
 
-def barrier(dist):
-    if dist is not None:
-        dist.barrier()
+def traffic_ratios():
+    """DRAM bytes per algorithmic byte of each kernel class, from the small-case
+    ncu capture summarised in profiles/roofline_traffic.json."""
+    tp = os.path.join(ROOT, "profiles", "roofline_traffic.json")
+    try:
+        d = json.load(open(tp))
+    except (OSError, ValueError):
+        return {}, None
+    return d.get("dram_bytes_per_algorithmic_byte", {}), d.get("case")
 
 
 # ---------------------------------------------------------------------- workload
+def config_dict(idx, stats_list, nbfs):
+    """Workload description shared by both arms (same keys and values)."""
+    d = dict(workload=WORKLOADS.get(idx, str(idx)), config_index=idx,
+             nbf=int(max(nbfs)) if len(nbfs) == 1 else int(sum(nbfs)),
+             ntasks=int(sum(s["ntasks"] for s in stats_list)),
+             npts=int(sum(s["npts"] for s in stats_list)),
+             l2=l2_note(sum(n * n * 8 for n in nbfs)))
+    if len(nbfs) > 1:
+        d["members"] = len(nbfs)
+    return d
+
+
+def l2_note(pbytes):
+    state = ("larger than the 129 MB L2, no flush needed" if 2 * pbytes > 129e6
+             else "within L2 (small case)")
+    return f"P and VXC {pbytes / 1e9:.2f} GB each per step, {state}"
+
+
+def host_stats(lb):
+    infos = [lb.task_info(i) for i in range(lb.ntasks())]
+    return dict(ntasks=len(infos), npts=sum(i["npts"] for i in infos)), infos
+
+
 def setup_workload(cfg_idx, lwd):
     import gauxc_gb300 as g
     from gauxc_gb300 import workloads as W
@@ -140,15 +193,13 @@ def setup_workload(cfg_idx, lwd):
     t0 = time.perf_counter()
     mol, basis, mg, lb = W.build_system(s)
     t_lb = time.perf_counter() - t0
-    tasks0 = None
     t0 = time.perf_counter()
     mw = g.MolecularWeightsFactory(g.ExecutionSpace.Device).get_instance()
     mw.modify_weights(lb)
     t_w = time.perf_counter() - t0
     integ = g.XCIntegratorFactory(g.ExecutionSpace.Device, "Replicated", "Default", lwd,
                                   "Default").get_instance(g.functional_type(s["functional"]), lb)
-    return dict(cfg=cfg, sys=s, mol=mol, basis=basis, lb=lb, integ=integ, t_lb=t_lb, t_w=t_w,
-                tasks0=tasks0)
+    return dict(cfg=cfg, sys=s, mol=mol, basis=basis, lb=lb, integ=integ, t_lb=t_lb, t_w=t_w)
 
 
 def pinned_like(P):
@@ -163,7 +214,7 @@ def pinned_like(P):
         pinned = True
     except Exception:
         pinned = False
-    return a, v, pinned, (a, v)
+    return a, v, pinned
 
 
 def eval_into(integ, P, V):
@@ -182,40 +233,117 @@ def eval_into(integ, P, V):
 
 
 # ---------------------------------------------------------------------- CPU baseline
-def cpu_sample(lb, target_frac):
+def cpu_sample(infos, target_frac):
     """Deterministic strided sample of the tasks (reference order: npts*nbe desc)."""
-    infos = [lb.task_info(i) for i in range(lb.ntasks())]
     order = sorted(range(len(infos)), key=lambda i: -infos[i]["npts"] * infos[i]["nbe"])
     stride = max(1, int(round(1.0 / target_frac)))
-    pick = order[::stride]
+    pick = sorted(order[::stride])
     cost = np.array([infos[i]["npts"] * infos[i]["nbe"] ** 2 for i in range(len(infos))], float)
     return pick, cost[pick].sum() / cost.sum()
 
 
-def time_cpu(W, basis, lb, P, func, budget_s=15.0, nthreads=0):
-    """Oracle on growing strided samples until one takes >= budget/4; extrapolate."""
+class WeightedSample:
+    """Tasks of a strided sample with SSF weights from the oracle (host
+    algorithm), computed once for the sampled points only."""
+
+    def __init__(self, lb, coords, pick):
+        import oracle
+        self.tasks = []
+        for i in pick:
+            t = lb.task(i)
+            n = t["npts"]
+            w = oracle.ssf_weights(t["points"], np.full(n, t["iParent"], np.int32),
+                                   np.full(n, t["dist_nearest"]), coords, t["weights"])
+            self.tasks.append((t["points"], w, t["shell_list"]))
+
+
+def choose_sample(infos, ob, lb, coords, P, func, budget_s):
+    """Grows a strided sample until one oracle pass takes >= budget_s / 2."""
+    import oracle
+    frac = 1.0 / 1024
+    while True:
+        pick, share = cpu_sample(infos, frac)
+        ws = WeightedSample(lb, coords, pick)
+        t0 = time.perf_counter()
+        oracle.eval_exc_vxc(ob, ws.tasks, P, func)
+        dt = time.perf_counter() - t0
+        if dt >= budget_s / 2 or frac >= 1.0:
+            return ws, pick, share, dt
+        frac = min(1.0, frac * max(2.0, min(8.0, (budget_s / 2) / max(dt, 1e-3))))
+
+
+def oracle_basis(basis):
     import oracle
     l, pure, nprim, alpha, coeff, origin, _ = basis.arrays()
-    ob = oracle.Basis(l, pure, nprim, alpha, coeff, origin)
-    frac = 1.0 / 512
-    while True:
-        pick, share = cpu_sample(lb, frac)
-        tasks = [lb.task(i) for i in pick]
-        ot = [(t["points"], t["weights"], t["shell_list"]) for t in tasks]
+    return oracle.Basis(l, pure, nprim, alpha, coeff, origin)
+
+
+def cpu_leg(basis, lb, mol, P, func, budget_s, infos=None):
+    """One bounded oracle sample of the workload, extrapolated."""
+    import oracle
+    if infos is None:
+        infos = [lb.task_info(i) for i in range(lb.ntasks())]
+    ob = oracle_basis(basis)
+    ws, pick, share, dt = choose_sample(infos, ob, lb, mol.coords(), P, func, budget_s)
+    return dict(ws=ws, ob=ob, pick=pick, share=share, dt=dt, est=dt / share,
+                blas=oracle.blas_active())
+
+
+# ---------------------------------------------------------------------- reference arm
+def run_reference(args, ncores):
+    """The reference's host algorithm (oracle port, BLAS contractions) on the
+    host cores, on a fixed strided sample of the workload's tasks."""
+    import oracle
+    from gauxc_gb300 import workloads as W
+    cfg = W.config(args.config)
+    systems = cfg["systems"]
+    built = [(sd,) + tuple(W.build_system(sd, device=False)) for sd in systems]
+    stats, nbfs, costs, all_infos = [], [], [], []
+    for sd, mol, basis, mg, lb in built:
+        st, infos = host_stats(lb)
+        stats.append(st)
+        nbfs.append(sd["nbf"])
+        costs.append(sum(i["npts"] * i["nbe"] ** 2 for i in infos))
+        all_infos.append(infos)
+    # the largest system is timed; the others count by their share of
+    # sum npts*nbe^2 (batched workload)
+    k = int(np.argmax(costs))
+    scale = sum(costs) / costs[k]
+    sd, mol, basis, mg, lb = built[k]
+    leg = cpu_leg(basis, lb, mol, sd["P"], sd["functional"], args.cpu_budget / 2, all_infos[k])
+    times = []
+    for it in range(args.warmup + args.steps):
         t0 = time.perf_counter()
-        oracle.eval_exc_vxc(ob, ot, P, func, nthreads=nthreads)
+        oracle.eval_exc_vxc(leg["ob"], leg["ws"].tasks, sd["P"], sd["functional"])
         dt = time.perf_counter() - t0
-        if dt >= budget_s / 4 or frac >= 1.0:
-            return dt / share, dt, len(pick), share
-        frac = min(1.0, frac * max(2.0, min(8.0, (budget_s / 4) / max(dt, 1e-3))))
+        if it >= args.warmup:
+            times.append(dt / leg["share"] * scale)
+    v = float(np.mean(times))
+    sample = (f"{len(leg['pick'])} of {len(all_infos[k])} tasks of the "
+              f"{'largest member' if len(built) > 1 else 'system'} (every "
+              f"{max(1, round(len(all_infos[k]) / max(len(leg['pick']), 1)))}th in npts*nbe order) = "
+              f"{leg['share']:.4f} of its sum npts*nbe^2, {np.mean(times) * leg['share'] / scale:.2f} s "
+              f"per step, extrapolated by that share" + (f" and x{scale:.2f} for all members"
+                                                          if len(built) > 1 else ""))
+    line = dict(metric=METRIC, value=v, unit="s", n_gpus=args.gpus, steps=args.steps,
+                warmup=args.warmup, ms_per_step=v * 1e3, higher_is_better=False,
+                scaling="weak", vs_baseline=None, dtype="f64",
+                data="synthetic: seeded water clusters, even-tempered basis, P=CC^T (no dataset)",
+                config=config_dict(args.config, stats, nbfs), impl="reference",
+                cpu_baseline=dict(value=v, unit="s", cores=ncores, kind="port",
+                                  cpu=cpu_model(), blas=bool(leg["blas"]), sample=sample,
+                                  extrapolated=True),
+                e2e=dict(value=v, unit="s", h2d_bytes_per_step=0, d2h_bytes_per_step=0))
+    print(json.dumps(line), flush=True)
+    return 0
 
 
 # ---------------------------------------------------------------------- batched
-def run_batched(args, dist, rank, local, ncores):
+def run_batched(args, ncores):
     """The batched workload: every cluster's EXC+VXC in one graph launch."""
     import gauxc_gb300 as g
     from gauxc_gb300 import workloads as W
-    g.set_device(local)
+    g.set_device(0)
     cfg = W.config(args.config)
     t0 = time.perf_counter()
     systems = []
@@ -253,8 +381,7 @@ def run_batched(args, dist, rank, local, ncores):
     batch = g.IntegratorBatch(integs)
     for _ in range(max(args.warmup, 2)):  # the first call captures the graph
         batch.eval_exc_vxc(Ps, Vs)
-    sampler = ClockSampler(local)
-    barrier(dist)
+    sampler = ClockSampler(0)
     sampler.start()
     comp, wall = [], []
     t_all0 = time.perf_counter()
@@ -262,39 +389,31 @@ def run_batched(args, dist, rank, local, ncores):
         t0 = time.perf_counter()
         exc = batch.eval_exc_vxc(Ps, Vs)
         wall.append(time.perf_counter() - t0)
-        tm = batch.timings()
-        comp.append(tm["compute_ms"] * 1e-3)
+        comp.append(batch.timings()["compute_ms"] * 1e-3)
     t_all = time.perf_counter() - t_all0
-    barrier(dist)
     clocks = sampler.stop()
-    value = reduce_max(dist, float(np.mean(comp)))
-    e2e = reduce_max(dist, float(np.mean(wall)))
-    if rank != 0:
-        return 0
+    value = float(np.mean(comp))
+    e2e = float(np.mean(wall))
     stats = [i.plan_stats() for i in integs]
     nbfs = [P.shape[0] for P in Ps]
     launches = int(batch.timings()["gpu_launches"])
+    s2 = sum(st["sum_npts_nbe2"] for st in stats)
     if mixed:
-        peaks = {}
-        pp = os.path.join(ROOT, "MEASURED_PEAKS.json")
-        if os.path.exists(pp):
-            peaks = json.load(open(pp))
-        peak = peaks.get("bf16_tflops_sustained")
-        src = "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)"
-        if peak is None:
-            peak, src = 1700.0, "fallback sustained bf16 1.7 PFLOP/s (of fallback)"
-        fl = sum(st["tensor_flops_x"] + st["tensor_flops_v"] for st in stats)
-        achieved = fl / value / 1e12
+        peak, src = tensor_peak()
+        alg = SLICE_PAIRS * 4.0 * s2
+        issued = sum(st["tensor_flops_x"] + st["tensor_flops_v"] for st in stats)
         roofline = dict(bound="tensor", kernel="whole graph (all stages of all members)",
-                        achieved=achieved, peak=peak, unit="TFLOP/s", frac=achieved / peak,
-                        traffic=None, peak_source=src, algorithmic_flops_per_step=fl)
+                        achieved=alg / value / 1e12, peak=peak, unit="TFLOP/s",
+                        frac=alg / value / 1e12 / peak, traffic=None, peak_source=src,
+                        algorithmic_flops_per_step=alg, issued_flops_per_step=issued,
+                        issued_over_algorithmic=issued / alg)
     else:
         fp64_peak = g.measure_fp64_peak()
-        fl = sum(4.0 * st["sum_npts_nbe2"] for st in stats)
-        achieved = fl / value / 1e12
+        fl = 4.0 * s2
         roofline = dict(bound="fp64", kernel="whole graph (all stages of all members)",
-                        achieved=achieved, peak=fp64_peak, unit="TFLOP/s", frac=achieved / fp64_peak,
-                        traffic=None, peak_source="FP64 FMA probe measured in this run",
+                        achieved=fl / value / 1e12, peak=fp64_peak, unit="TFLOP/s",
+                        frac=fl / value / 1e12 / fp64_peak, traffic=None,
+                        peak_source="FP64 FMA probe measured in this run",
                         algorithmic_flops_per_step=fl)
     fp64_check = None
     if mixed and not args.no_fp64_check:
@@ -311,29 +430,22 @@ def run_batched(args, dist, rank, local, ncores):
                           gates=dict(delta_exc=1e-8, max_delta_vxc=1e-8))
     cpu = None
     if not args.no_cpu_baseline:
-        # oracle on a sample of the largest member, scaled by sum npts*nbe^2
         k = int(np.argmax([st["sum_npts_nbe2"] for st in stats]))
         s, mol, basis, mg, lb = systems[k]
-        est, dt, ntask, share = time_cpu(W, basis, lb, s["P"], s["functional"],
-                                         budget_s=args.cpu_budget)
-        tot = sum(st["sum_npts_nbe2"] for st in stats)
-        scale = tot / stats[k]["sum_npts_nbe2"]
-        cpu = dict(value=est * scale, unit="s", cores=ncores, kind="port",
-                   sample=f"{ntask} tasks of the largest cluster ({share:.4f} of its sum "
-                          f"npts*nbe^2, {dt:.1f} s), scaled to all {len(systems)} clusters by "
-                          f"sum npts*nbe^2")
+        leg = cpu_leg(basis, lb, mol, s["P"], s["functional"], args.cpu_budget)
+        scale = s2 / stats[k]["sum_npts_nbe2"]
+        cpu = dict(value=leg["est"] * scale, unit="s", cores=os.cpu_count() or 1, kind="port",
+                   cpu=cpu_model(), blas=bool(leg["blas"]),
+                   sample=f"{len(leg['pick'])} tasks of the largest cluster ({leg['share']:.4f} "
+                          f"of its sum npts*nbe^2, {leg['dt']:.1f} s), scaled to all "
+                          f"{len(systems)} clusters by sum npts*nbe^2", extrapolated=True)
     line = dict(
-        metric=METRIC, value=value, unit="s", n_gpus=args.gpus, steps=args.steps,
+        metric=METRIC, value=value, unit="s", n_gpus=1, steps=args.steps,
         warmup=args.warmup, ms_per_step=value * 1e3, higher_is_better=False, scaling="weak",
         vs_baseline=None,
         dtype="bf16 digits (6 x 7 bit FP64 emulation, FP64 accumulate)" if mixed else "f64",
         data="synthetic: seeded water clusters, even-tempered basis, P=CC^T (no dataset)",
-        config=dict(workload=WORKLOADS[args.config], config_index=args.config, lwd=args.lwd,
-                    members=len(systems), nbf_total=int(sum(nbfs)), nbf_max=int(max(nbfs)),
-                    npts=int(sum(st["npts"] for st in stats)),
-                    ntasks=int(sum(st["ntasks"] for st in stats)),
-                    l2="inputs larger than L2 (sum of members' P and VXC)",
-                    parallelism=f"replicas x{args.gpus}"),
+        config=config_dict(args.config, stats, nbfs), path=dict(lwd=args.lwd, parallelism="1 GPU"),
         e2e=dict(value=e2e, unit="s", h2d_bytes_per_step=int(sum(n * n * 8 for n in nbfs)),
                  d2h_bytes_per_step=int(sum(n * n * 8 + 16 for n in nbfs)), pinned=True),
         roofline=roofline, cpu_baseline=cpu, gpu_launches=launches,
@@ -356,84 +468,51 @@ def main():
     # with the FP64 device path timed beside it for the speed-up and the errors
     ap.add_argument("--config", type=int, default=4)
     ap.add_argument("--lwd", default="GB300-Mixed")
-    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--cpu-budget", type=float, default=16.0)
+    ap.add_argument("--scratch-gb", type=float, default=0.0,
+                    help="cap of the plan's work space per pass (0 = from free memory)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-check", action="store_true",
                     help="mixed path: skip the FP64 device pass used for dEXC / dVXC")
     ap.add_argument("--no-autotune", action="store_true",
                     help="batched workload: keep the default plan parameters")
     args = ap.parse_args()
-    ws, rank, local = dist_env()
-    dist = init_dist(ws)
-    if ws > 1:
-        # cluster multicast of GEMM operands only in single-GPU runs
-        os.environ.setdefault("GAUXC_GB300_CLUSTER_MULTICAST", "0")
-
-    import gauxc_gb300 as g
-    from gauxc_gb300 import workloads as W
-
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
     ncores = os.cpu_count() or 1
+
     if args.impl == "reference":
-        if rank != 0:
-            return 0
-        systems = W.config(args.config)["systems"]
-        scale = 1.0
-        if len(systems) > 1:
-            # batched workload: the largest cluster is timed, the others are
-            # accounted for by sum npts*nbe^2 of their (host-built) task lists
-            costs = []
-            for sd in systems:
-                lbx = W.build_system(sd, device=False)[3]
-                costs.append(sum(lbx.task_info(i)["npts"] * lbx.task_info(i)["nbe"] ** 2
-                                 for i in range(lbx.ntasks())))
-            k = int(np.argmax(costs))
-            scale = sum(costs) / costs[k]
-            s = systems[k]
-        else:
-            s = systems[0]
-        mol, basis, mg, lb = W.build_system(s, device=False)
-        # the reference integrator needs weighted tasks: SSF by the CPU oracle,
-        # for the points of the sampled tasks only
-        lbw = _SampledWeightedTasks(lb, mol)
-        times = []
-        for it in range(args.warmup + args.steps):
-            est, dt, ntask, share = time_cpu(W, basis, lbw, s["P"], s["functional"],
-                                             budget_s=args.cpu_budget / 2)
-            if it >= args.warmup:
-                times.append(est * scale)
-        v = float(np.mean(times))
-        line = dict(metric=METRIC, value=v, unit="s", n_gpus=args.gpus, steps=args.steps,
-                    warmup=args.warmup, ms_per_step=v * 1e3, higher_is_better=False,
-                    scaling="weak", vs_baseline=None, dtype="f64",
-                    data="synthetic: seeded water cluster, even-tempered basis, P=CC^T",
-                    config=dict(workload=WORKLOADS.get(args.config, str(args.config)),
-                                config_index=args.config),
-                    impl="reference",
-                    cpu_baseline=dict(value=v, unit="s", cores=ncores, kind="port",
-                                      sample=f"{ntask} of {lb.ntasks()} tasks (strided over the "
-                                             f"npts*nbe order), {share:.4f} of sum npts*nbe^2, "
-                                             f"extrapolated"),
-                    e2e=dict(value=v, unit="s", h2d_bytes_per_step=0, d2h_bytes_per_step=0))
-        print(json.dumps(line), flush=True)
+        # CPU only: under torchrun rank 0 alone runs it
+        return run_reference(args, ncores) if rank == 0 else 0
+
+    if ws > 1 or args.gpus > 1:
+        if rank == 0:
+            print(json.dumps(dict(metric=METRIC, impl="gb300", n_gpus=max(ws, args.gpus),
+                                  unavailable="single-GPU path: the XC integrator runs on one "
+                                              "GPU per process (replicas only, no multi-GPU "
+                                              "mode)")), flush=True)
         return 0
 
-    if args.config == 3:
-        return run_batched(args, dist, rank, local, ncores)
+    import gauxc_gb300 as g
 
-    g.set_device(local)
+    if args.config == 3:
+        return run_batched(args, ncores)
+
+    g.set_device(0)
     ctx = setup_workload(args.config, args.lwd)
     integ, s = ctx["integ"], ctx["sys"]
-    P, V, pinned, _keep = pinned_like(s["P"])
+    if args.scratch_gb > 0:
+        integ.set_plan_params(scratch_gb=args.scratch_gb)
+    P, V, pinned = pinned_like(s["P"])
     nbf = s["nbf"]
-    stats = integ.plan_stats()
 
     for _ in range(args.warmup):
         eval_into(integ, P, V)
+    stats = integ.plan_stats()
     fp64_peak = g.measure_fp64_peak()
     integ.set_profiling(True)
 
-    sampler = ClockSampler(local)
-    barrier(dist)
+    sampler = ClockSampler(0)
     sampler.start()
     comp, wall, launches = [], [], 0
     kt, brk = {}, {}
@@ -446,63 +525,73 @@ def main():
         comp.append(tm["compute_ms"] * 1e-3)
         for k in ("h2d_ms", "compute_ms", "d2h_ms", "wall_ms"):
             brk.setdefault(k, []).append(tm.get(k, 0.0))
-        st = integ.plan_stats()
-        launches += int(st["gpu_launches"])
+        launches += int(integ.plan_stats()["gpu_launches"])
         for k, v in integ.kernel_times().items():
             e = kt.setdefault(k, dict(ms=0.0, launches=0))
             e["ms"] += v["ms"]
             e["launches"] += v["launches"]
     t_all = time.perf_counter() - t_all0
-    barrier(dist)
     clocks = sampler.stop()
     integ.set_profiling(False)
+    value = float(np.mean(comp))
+    e2e = float(np.mean(wall))
 
-    value = reduce_max(dist, float(np.mean(comp)))
-    e2e = reduce_max(dist, float(np.mean(wall)))
-    if rank != 0:
-        return 0
-
-    # roofline of the dominant kernel class
+    # ---- roofline of the dominant kernel class (algorithmic work)
     mixed = args.lwd.lower() == "gb300-mixed"
     gga = s["functional"] != "SVWN5"
     dom = "density" if kt["density"]["ms"] >= kt["vxc"]["ms"] else "vxc"
-    dom_s = kt[dom]["ms"] * 1e-3
-    f_x = 2.0 * stats["sum_npts_nbe2"] + 2.0 * stats["sum_npts_nbe"] * (4 if gga else 1)
-    f_v = 2.0 * stats["sum_npts_nbe2"]
-    f64_flops = (f_x if dom == "density" else f_v) * args.steps
+    dom_s = kt[dom]["ms"] * 1e-3 / args.steps
+    n_launch = kt[dom]["launches"] / args.steps
+    s2, s1 = stats["sum_npts_nbe2"], stats["sum_npts_nbe"]
+    # FP64 work of the contraction: X = 2 phi P (2 npts nbe^2) or the
+    # symmetric rank-2k phi^T Z + Z^T phi on the triangle (2 npts nbe^2)
+    f64_alg = 2.0 * s2
+    ratios, case = traffic_ratios()
+    kb = stats["kernel_bytes"]
     traffic = None
-    tp = os.path.join(ROOT, "profiles", "roofline_traffic.json")
-    if os.path.exists(tp):
-        try:
-            traffic = json.load(open(tp)).get(f"config{args.config}_{args.lwd}_{dom}")
-        except (ValueError, OSError):
-            traffic = None
+    if mixed and ratios.get(dom):
+        traffic = ratios[dom] * kb[dom] / max(n_launch, 1)
     if mixed:
-        peaks = {}
-        pp = os.path.join(ROOT, "MEASURED_PEAKS.json")
-        if os.path.exists(pp):
-            peaks = json.load(open(pp))
-        peak = peaks.get("bf16_tflops_sustained")
-        src = "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)"
-        if peak is None:
-            peak, src = 1700.0, "fallback sustained bf16 1.7 PFLOP/s (of fallback)"
-        tflops = (stats["tensor_flops_x"] if dom == "density" else stats["tensor_flops_v"]) * args.steps
-        achieved = tflops / dom_s / 1e12
-        roofline = dict(bound="tensor", kernel=f"ozaki_kernel<{'X' if dom == 'density' else 'V'}>",
-                        achieved=achieved, peak=peak, unit="TFLOP/s", frac=achieved / peak,
-                        traffic=traffic, peak_source=src,
-                        traffic_note=("DRAM read+write bytes per launch (ncu launch list, "
-                                      "profiles/launches_mixed_256water.md)" if traffic else None),
-                        launches_per_step=kt[dom]["launches"] / args.steps,
-                        algorithmic_flops_per_step=tflops / args.steps,
-                        fp64_equivalent_tflops=f64_flops / dom_s / 1e12)
+        peak, src = tensor_peak()
+        alg = SLICE_PAIRS * f64_alg
+        issued = stats["tensor_flops_x"] if dom == "density" else stats["tensor_flops_v"]
+        roofline = dict(
+            bound="tensor", kernel=f"ozaki_kernel<{'X' if dom == 'density' else 'V'}>",
+            achieved=alg / dom_s / 1e12, peak=peak, unit="TFLOP/s",
+            frac=alg / dom_s / 1e12 / peak, traffic=traffic, peak_source=src,
+            work=f"{SLICE_PAIRS} BF16 slice-pair products x 2 sum(npts nbe^2) FP64 flops per call "
+                 "(task nbe, unpadded)",
+            algorithmic_flops_per_step=alg, issued_flops_per_step=issued,
+            issued_over_algorithmic=issued / alg, issued_frac=issued / dom_s / 1e12 / peak,
+            launches_per_step=n_launch, fp64_equivalent_tflops=f64_alg / dom_s / 1e12,
+            traffic_algorithmic=kb[dom] / max(n_launch, 1),
+            traffic_source=(f"DRAM read+write bytes per algorithmic byte of this kernel from an "
+                            f"ncu capture of {case}, times this launch's algorithmic bytes"
+                            if traffic else None))
     else:
-        achieved = f64_flops / dom_s / 1e12
-        roofline = dict(bound="fp64", kernel=dom, achieved=achieved, peak=fp64_peak,
-                        unit="TFLOP/s", frac=achieved / fp64_peak, traffic=traffic,
-                        peak_source="FP64 FMA probe measured in this run (no FP64 figure in the "
-                                    "measured-peaks file)",
-                        algorithmic_flops_per_step=f64_flops / args.steps)
+        roofline = dict(bound="fp64", kernel=dom, achieved=f64_alg / dom_s / 1e12,
+                        peak=fp64_peak, unit="TFLOP/s", frac=f64_alg / dom_s / 1e12 / fp64_peak,
+                        traffic=None, peak_source="FP64 FMA probe measured in this run (no FP64 "
+                                                  "figure in the measured-peaks file)",
+                        algorithmic_flops_per_step=f64_alg)
+
+    kernels = {}
+    for k, v in kt.items():
+        ms = v["ms"] / args.steps
+        e = dict(ms_per_step=ms, launches_per_step=v["launches"] / args.steps)
+        if kb.get(k):
+            e["algorithmic_bytes_per_step"] = kb[k]
+            if ms > 0:
+                e["algorithmic_gbs"] = kb[k] / (ms * 1e-3) / 1e9
+            if mixed and ratios.get(k):
+                e["dram_bytes_per_step_est"] = ratios[k] * kb[k]
+        kernels[k] = e
+    if mixed:
+        for k, key in (("density", "tensor_flops_x"), ("vxc", "tensor_flops_v")):
+            if k in kernels and kt[k]["ms"] > 0:
+                t = kt[k]["ms"] * 1e-3 / args.steps
+                kernels[k]["tensor_tflops_issued"] = stats[key] / t / 1e12
+                kernels[k]["tensor_tflops_algorithmic"] = SLICE_PAIRS * f64_alg / t / 1e12
 
     fp64_check = None
     if mixed and not args.no_fp64_check:
@@ -518,90 +607,37 @@ def main():
                           delta_nel=abs(integ.last_nel() - i64.last_nel()),
                           fp64_value=t64, speedup_vs_fp64=t64 / value,
                           gates=dict(delta_exc=1e-8, max_delta_vxc=1e-8))
+        i64 = None
 
     cpu = None
     if not args.no_cpu_baseline:
-        est, dt, ntask, share = time_cpu(W, ctx["basis"], ctx["lb"], s["P"], s["functional"],
-                                         budget_s=args.cpu_budget)
-        cpu = dict(value=est, unit="s", cores=ncores, kind="port",
-                   sample=f"{ntask} of {int(stats['ntasks'])} tasks (strided over the npts*nbe "
-                          f"order) = {share:.4f} of sum npts*nbe^2, {dt:.1f} s, extrapolated")
+        leg = cpu_leg(ctx["basis"], ctx["lb"], ctx["mol"], s["P"], s["functional"],
+                      args.cpu_budget)
+        cpu = dict(value=leg["est"], unit="s", cores=ncores, kind="port", cpu=cpu_model(),
+                   blas=bool(leg["blas"]),
+                   sample=f"{len(leg['pick'])} of {int(stats['ntasks'])} tasks (strided over the "
+                          f"npts*nbe order) = {leg['share']:.4f} of sum npts*nbe^2, "
+                          f"{leg['dt']:.1f} s, extrapolated by that share", extrapolated=True)
 
     line = dict(
-        metric=METRIC, value=value, unit="s", n_gpus=args.gpus, steps=args.steps,
+        metric=METRIC, value=value, unit="s", n_gpus=1, steps=args.steps,
         warmup=args.warmup, ms_per_step=value * 1e3, higher_is_better=False, scaling="weak",
         vs_baseline=None,
         dtype="bf16 digits (6 x 7 bit FP64 emulation, FP64 accumulate)" if mixed else "f64",
         data="synthetic: seeded water cluster, even-tempered basis, P=CC^T (no dataset)",
-        config=dict(workload=WORKLOADS.get(args.config, str(args.config)), config_index=args.config,
-                    lwd=args.lwd, nbf=nbf, ntasks=int(stats["ntasks"]), npts=int(stats["npts"]),
-                    nbatches=int(stats["nbatches"]),
-                    l2="inputs larger than L2 (scratch %.1f GB per batch)" % (stats["scratch_bytes"] / 1e9),
-                    parallelism=f"replicas x{args.gpus}"),
+        config=config_dict(args.config, [stats], [nbf]),
+        path=dict(lwd=args.lwd, parallelism="1 GPU", nbatches=int(stats["nbatches"]),
+                  scratch_gb=stats["scratch_bytes"] / 1e9),
         e2e=dict(value=e2e, unit="s", h2d_bytes_per_step=nbf * nbf * 8,
                  d2h_bytes_per_step=nbf * nbf * 8 + 16, pinned=pinned,
                  breakdown_ms={k: float(np.mean(v)) for k, v in brk.items()}),
         roofline=roofline, cpu_baseline=cpu, gpu_launches=launches, clocks=clocks,
-        fp64_check=fp64_check,
-        exc=exc, nel=integ.last_nel(),
-        grid_points_bf_per_s=stats["sum_npts_nbe"] / value,
-        kernels={k: dict(ms_per_step=v["ms"] / args.steps, launches_per_step=v["launches"] / args.steps)
-                 for k, v in kt.items()},
+        fp64_check=fp64_check, exc=exc, nel=integ.last_nel(),
+        grid_points_bf_per_s=s1 / value, kernels=kernels,
         setup_s=dict(load_balancer=ctx["t_lb"], ssf_weights=ctx["t_w"]),
         timed_wall_s=t_all)
-    if mixed:
-        for k, key in (("density", "tensor_flops_x"), ("vxc", "tensor_flops_v")):
-            if k in line["kernels"] and kt[k]["ms"] > 0:
-                line["kernels"][k]["tensor_tflops"] = stats[key] * args.steps / (kt[k]["ms"] * 1e-3) / 1e12
     print(json.dumps(line), flush=True)
     return 0
-
-
-class _SampledWeightedTasks:
-    """Load-balancer view whose task() applies SSF weights (CPU oracle) on
-    demand, so that only the tasks a CPU sample touches are weighted."""
-
-    def __init__(self, lb, mol):
-        self.lb, self.coords, self.cache = lb, mol.coords(), {}
-
-    def ntasks(self):
-        return self.lb.ntasks()
-
-    def task_info(self, i):
-        return self.lb.task_info(i)
-
-    def task(self, i):
-        if i not in self.cache:
-            import oracle
-            t = dict(self.lb.task(i))
-            n = t["npts"]
-            t["weights"] = oracle.ssf_weights(t["points"], np.full(n, t["iParent"], np.int32),
-                                              np.full(n, t["dist_nearest"]), self.coords,
-                                              t["weights"])
-            self.cache[i] = t
-        return self.cache[i]
-
-
-class _WeightedTasks:
-    """Load-balancer-like view of tasks with replaced weights (CPU reference arm)."""
-
-    def __init__(self, tasks, weights):
-        self.tasks = []
-        o = 0
-        for t in tasks:
-            t = dict(t)
-            t["weights"] = weights[o:o + t["npts"]]
-            o += t["npts"]
-            self.tasks.append(t)
-
-    def ntasks(self):
-        return len(self.tasks)
-
-    def task_info(self, i):
-        return self.tasks[i]
-
-    def task(self, i):
-        return self.tasks[i]
 
 
 if __name__ == "__main__":

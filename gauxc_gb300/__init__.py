@@ -320,6 +320,15 @@ class LoadBalancer(_Handle):
     def weights_modified(self):
         return bool(_call(_L.gauxc_gb300_load_balancer_weights_modified, self._h))
 
+    def subset(self, task_indices):
+        """A load balancer over the listed tasks (copies, current weights)."""
+        idx = np.ascontiguousarray(task_indices, dtype=np.int64)
+        lb = LoadBalancer(_call(_L.gauxc_gb300_load_balancer_subset, self._h,
+                                idx.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                ctypes.c_size_t(len(idx))))
+        lb._keep = self._keep
+        return lb
+
 
 class LoadBalancerFactory(_Handle):
     _delete = "gauxc_load_balancer_factory_delete"
@@ -416,6 +425,13 @@ class XCIntegrator(_Handle):
     def set_profiling(self, on=True):
         _call(_L.gauxc_gb300_integrator_set_profiling, self._h, ctypes.c_bool(on))
 
+    def set_pipeline_check(self, wait_ms=1000.0, withhold=False):
+        """Bound of the tensor-core pipeline waits (ms) of the following calls;
+        withhold=True makes the GEMM producers issue no copy, so the calls fail
+        with the pipeline error after wait_ms (check of the error path)."""
+        _call(_L.gauxc_gb300_integrator_set_pipeline_check, self._h, ctypes.c_double(wait_ms),
+              ctypes.c_bool(withhold))
+
     def kernel_times(self):
         out = (ctypes.c_double * 14)()
         _call(_L.gauxc_gb300_integrator_kernel_times, self._h, out, 14)
@@ -423,12 +439,15 @@ class XCIntegrator(_Handle):
         return {n: dict(ms=out[2 * i], launches=int(out[2 * i + 1])) for i, n in enumerate(names)}
 
     def plan_stats(self):
-        out = (ctypes.c_double * 11)()
-        _call(_L.gauxc_gb300_integrator_plan_stats, self._h, out, 11)
+        out = (ctypes.c_double * 18)()
+        _call(_L.gauxc_gb300_integrator_plan_stats, self._h, out, 18)
         keys = ["ntasks", "npts", "npts_pad", "nbatches", "sum_npts_nbe", "sum_npts_nbe2",
                 "sum_pad_npts_nbe2", "scratch_bytes", "gpu_launches", "tensor_flops_x",
                 "tensor_flops_v"]
-        return dict(zip(keys, list(out)))
+        st = dict(zip(keys, list(out)))
+        names = ["collocation", "density", "zmat", "vxc", "other", "phi_digits", "p_digits"]
+        st["kernel_bytes"] = {n: out[11 + i] for i, n in enumerate(names)}
+        return st
 
 
     def set_plan_params(self, pb_max_pts=256, nu2_weight=300.0, scratch_gb=0.0):

@@ -110,6 +110,7 @@ PROTOTYPES = {
     "gauxc_gb300_load_balancer_task_data": (None, [S, GauXCLoadBalancer, sz, P(dbl), P(dbl),
                                                    P(i32)]),
     "gauxc_gb300_load_balancer_weights_modified": (b, [S, GauXCLoadBalancer]),
+    "gauxc_gb300_load_balancer_subset": (GauXCLoadBalancer, [S, GauXCLoadBalancer, P(i64), sz]),
     "gauxc_gb300_integrator_last_nel": (dbl, [S, GauXCIntegrator]),
     "gauxc_gb300_integrator_timings": (I, [S, GauXCIntegrator, P(dbl), I]),
     "gauxc_gb300_integrator_plan_stats": (I, [S, GauXCIntegrator, P(dbl), I]),
@@ -122,6 +123,7 @@ PROTOTYPES = {
     "gauxc_gb300_batch_timings": (I, [S, GauXCGB300Batch, P(dbl), I]),
     "gauxc_gb300_batch_delete": (None, [S, P(GauXCGB300Batch)]),
     "gauxc_gb300_integrator_set_profiling": (None, [S, GauXCIntegrator, b]),
+    "gauxc_gb300_integrator_set_pipeline_check": (None, [S, GauXCIntegrator, dbl, b]),
     "gauxc_gb300_integrator_kernel_times": (I, [S, GauXCIntegrator, P(dbl), I]),
     "gauxc_gb300_measure_fp64_peak": (dbl, [S]),
     "gauxc_gb300_host_register": (ctypes.c_int, [S, ctypes.c_void_p, ctypes.c_size_t]),

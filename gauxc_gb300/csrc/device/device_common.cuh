@@ -59,10 +59,14 @@ constexpr int kPtBlock = 64;   // point padding / density tile rows
 constexpr int kBfBlock = 64;   // basis padding / tile columns
 
 // ---------------------------------------------------------------- launchers
+// SSF weights of npts points (reference algorithm, cuda_ssf_1d.cu:24-131);
+// status (may be null) is set to 1 when a parent index lies outside
+// [0, natoms), and that point keeps its weight.
 void launch_ssf_weights(int64_t npts, int natoms, const double* x, const double* y,
                         const double* z, const int32_t* iparent, const double* dist_nearest,
                         const double* coords, const double* rab_inv, int ld_rab,
-                        double* dist_scr, int ld_dist, double* weights, cudaStream_t s);
+                        double* dist_scr, int ld_dist, double* weights, int* status,
+                        cudaStream_t s);
 
 void launch_collocation(const ShellsDev& sh, const TasksDev& tk, const int2* items, int nitems,
                         double* scr, bool grad, cudaStream_t s);

@@ -112,8 +112,6 @@ class DeviceIntegrator {
       GB300_CUDA(cudaGetDevice(&dev));
       GB300_CUDA(cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, dev));
       host_direct_ = pma != 0;
-      const char* mc = std::getenv("GAUXC_GB300_CLUSTER_MULTICAST");
-      multicast_ = (mc && std::string(mc) == "0") ? 0 : 1;
     }
     for (auto& e : ev_) GB300_CUDA(cudaEventCreate(&e));
     build(lb);
@@ -128,6 +126,10 @@ class DeviceIntegrator {
   PlanStats stats;
   std::map<std::string, double> timings;
   bool profiling = false;
+  // tensor-core pipeline: bound of every wait, and the error-path check
+  // (producers issue no copy; see OzSchedule)
+  uint64_t wait_ns = kOzWaitNs;
+  bool withhold = false;
   // per kernel class: accumulated ms and launch count of the last call
   // collocation, density, zmat, vxc, other, phi digits (+ point scales), P digits
   double kclass_ms[7] = {0, 0, 0, 0, 0, 0, 0};
@@ -171,9 +173,6 @@ class DeviceIntegrator {
   double4* zcoef_ = nullptr;
   double2* partials_ = nullptr;
   bool host_direct_ = false;  // P / VXC moved by kernels (pageable memory access)
-  // A-operand multicast inside GEMM clusters; GAUXC_GB300_CLUSTER_MULTICAST=0
-  // turns it off (processes that share a run with other GPUs)
-  int multicast_ = 1;
   double* P_ = nullptr;
   double* A_ = nullptr;
   double* V_ = nullptr;
@@ -303,6 +302,17 @@ void DeviceIntegrator::build(const LoadBalancer& lb) {
     stats.sum_npts_nbe += (double)t.npts * t.nbe;
     stats.sum_npts_nbe2 += (double)t.npts * t.nbe * t.nbe;
     stats.sum_pad_npts_nbe2 += (double)npts_pad[i] * nbe_pad[i] * nbe_pad[i];
+    {
+      // algorithmic bytes: phi (and grad phi) written by the collocation and
+      // read by density, zmat (Z written) and vxc; P_sub read by the density
+      // kernel, the task's VXC block read-modify-written once
+      const double pe = (double)t.npts * t.nbe * 8.;
+      const double nq = gga_ ? 4. : 1.;
+      stats.kbytes[0] += nq * pe;
+      stats.kbytes[1] += nq * pe + 8. * t.nbe * t.nbe + 32. * t.npts;
+      stats.kbytes[2] += nq * pe + pe + 32. * t.npts;
+      stats.kbytes[3] += 2. * pe + 16. * t.nbe * t.nbe;
+    }
   }
   stats.ntasks = nt;
   stats.npts_pad = pts;
@@ -509,6 +519,21 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
     pts += npts_pad[i];
     stats.npts += b.npts;
     stats.sum_pad_npts_nbe2 += (double)npts_pad[i] * nu_pad[i] * nu_pad[i];
+    {
+      // algorithmic bytes of each kernel at this plan's sizes: phi as
+      // float-float pairs (8 B), digit operands 6 BF16 planes (12 B)
+      const PBDims d(npts_pad[i], nu[i]);
+      const double nq = gga_ ? 4. : 1.;
+      const double phi = 8. * d.np * d.nu128;
+      stats.kbytes[0] += nq * phi;                                          // collocation
+      stats.kbytes[5] += phi + 12. * ((double)d.nu128 * d.np + (double)d.nun * d.np +
+                                      (double)d.np * d.nu16);               // phi digits
+      stats.kbytes[6] += 8. * d.nu * d.nu + 12. * d.nu128 * d.nu16;         // P digits
+      stats.kbytes[1] += 12. * ((double)d.nu128 * d.nu16 + (double)d.np * d.nu16) + nq * phi +
+                         32. * d.np;                                        // density GEMM
+      stats.kbytes[2] += nq * phi + 32. * d.np + 12. * (double)(d.nu128 + d.nun) * d.np;  // Z digits
+      stats.kbytes[3] += 12. * (double)(d.nu128 + d.nun) * 2. * d.np + 8. * d.nu * d.nu;  // VXC GEMM
+    }
   }
   for (const auto& t : tasks) {
     stats.sum_npts_nbe += (double)t.npts * t.nbe;
@@ -675,7 +700,7 @@ int64_t DeviceIntegrator::eval_mixed_batches(bool do_vxc) {
       return (int64_t)1;
     });
     launches += timed(1, [&] {
-      launch_ozaki_x(tk_, mp_, OzSchedule{slots_, sched_ + b.x_sched, b.x_ncl, multicast_}, f64_, dig_, gga_,
+      launch_ozaki_x(tk_, mp_, OzSchedule{slots_, sched_ + b.x_sched, b.x_ncl, wait_ns, withhold ? 1 : 0}, f64_, dig_, gga_,
                      rho4_, err_, s);
       return (int64_t)1;
     });
@@ -689,7 +714,7 @@ int64_t DeviceIntegrator::eval_mixed_batches(bool do_vxc) {
       return (int64_t)2;
     });
     launches += timed(3, [&] {
-      launch_ozaki_v(tk_, mp_, OzSchedule{slots_, sched_ + b.v_sched, b.v_ncl, multicast_}, f64_, dig_, gga_,
+      launch_ozaki_v(tk_, mp_, OzSchedule{slots_, sched_ + b.v_sched, b.v_ncl, wait_ns, withhold ? 1 : 0}, f64_, dig_, gga_,
                      A_, nbf_, err_, s);
       return (int64_t)1;
     });
@@ -701,6 +726,8 @@ int64_t DeviceIntegrator::enqueue(const double* P, int64_t ldp, double* VXC, int
                                   double* en_host, int* err_host, bool do_vxc, bool events) {
   cudaStream_t s = stream_;
   const size_t row = (size_t)nbf_ * sizeof(double);
+  // the error flag of this call's pipeline waits starts clear
+  GB300_CUDA(cudaMemsetAsync(err_, 0, sizeof(int), s));
   if (events) GB300_CUDA(cudaEventRecord(ev_[0], s));
   if (host_direct_) {
     // the device reads the caller's (pageable or page-locked) P itself
@@ -816,6 +843,8 @@ void ensure_plan(XCIntegratorHandle& h) {
     h.dev = std::make_shared<DeviceIntegrator>(*h.lb, *h.func, h.prec, *h.rt, h.params);
   }
   h.dev->profiling = h.profiling;
+  h.dev->wait_ns = h.wait_ns;
+  h.dev->withhold = h.withhold;
 }
 void check_dims(const XCIntegratorHandle& h, int64_t m, int64_t n, int64_t ldp) {
   const int64_t nbf = h.lb->basis->nbf;
@@ -857,6 +886,16 @@ std::map<std::string, double> integrator_timings(const XCIntegratorHandle& h) {
 void integrator_set_profiling(XCIntegratorHandle& h, bool on) {
   h.profiling = on;
   if (h.dev) h.dev->profiling = on;
+}
+
+void integrator_set_pipeline_check(XCIntegratorHandle& h, double wait_ms, bool withhold) {
+  if (!(wait_ms > 0.) || wait_ms > 60000.) throw error("pipeline wait bound must lie in (0, 60000] ms");
+  h.wait_ns = (uint64_t)(wait_ms * 1e6);
+  h.withhold = withhold;
+  if (h.dev) {
+    h.dev->wait_ns = h.wait_ns;
+    h.dev->withhold = withhold;
+  }
 }
 
 std::vector<double> integrator_kernel_times(const XCIntegratorHandle& h) {

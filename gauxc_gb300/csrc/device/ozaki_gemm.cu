@@ -80,7 +80,6 @@ constexpr int kWorkWarps = kEpiWarps - 2;  // draining warps that also process (
 constexpr int kRedOffset = kStages * kStageBytes;  // per working warp: parked chunk / transposition
 constexpr int kHandOffset = kRedOffset + kWorkWarps * kChunkBytes;
 constexpr int kBarOffset = kHandOffset + 4 * kChunkBytes;  // the four quarter-1 chunks
-constexpr uint64_t kWaitLimit = 1000000000ull;  // ns a pipeline wait may take before it counts as failed
 constexpr uint16_t kClusterMask = (1u << kCluster) - 1;
 static_assert(kBK == 16, "one MMA (K = 16) per operand tile");
 static_assert(kABytes % (16 * 12) == 0, "A shares of 1/2, 1/3, 1/4 are 16-byte multiples");
@@ -115,9 +114,9 @@ __device__ __forceinline__ bool warp_failed(const Bars* B) {
   return __shfl_sync(0xffffffffu, f, 0) != 0;
 }
 
-// Bounded wait whose outcome is the same in every lane of the warp.
-__device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity) {
-  const bool ok = umma::mbar_wait(bar, parity, kWaitLimit);
+// Bounded wait (limit_ns) whose outcome is the same in every lane of the warp.
+__device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity, uint64_t limit_ns) {
+  const bool ok = umma::mbar_wait(bar, parity, limit_ns);
   return __all_sync(0xffffffffu, ok);
 }
 
@@ -229,7 +228,7 @@ __device__ __forceinline__ bool same_a(const OzItem& a, const OzItem& b) {
   return a.pb == b.pb && a.m0 == b.m0 && a.k0 == b.k0 && a.k1 == b.k1;
 }
 
-__device__ __forceinline__ SlotView view_of(const SlotItems& s, int rank, bool multicast) {
+__device__ __forceinline__ SlotView view_of(const SlotItems& s, int rank) {
   SlotView v;
 #pragma unroll
   for (int r = 0; r < kCluster; ++r)
@@ -241,7 +240,7 @@ __device__ __forceinline__ SlotView view_of(const SlotItems& s, int rank, bool m
   for (int r = 0; r < kCluster; ++r) {
     if (s.q[r].pb < 0) continue;
     v.uses = max(v.uses, (s.q[r].k1 - s.q[r].k0) / kBK);
-    if (v.it.pb >= 0 && (multicast || r == rank) && same_a(s.q[r], v.it))
+    if (v.it.pb >= 0 && same_a(s.q[r], v.it))
       v.mask |= (uint16_t)(1u << r);
   }
   v.part = __popc(v.mask & ((1u << rank) - 1));
@@ -263,6 +262,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int cl = blockIdx.x / kCluster;
   int beg = sched.slot_off[cl];
   const int end = sched.slot_off[cl + 1];
+  const uint64_t wl = sched.wait_ns;
 
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) {
@@ -292,11 +292,14 @@ __global__ void __launch_bounds__(kThreads, 1)
     SlotItems cur, nxt;
     if (beg < end) load_slot(sched.items, beg, cur);
     nxt = cur;
-    for (int sl = beg; sl < end; ++sl) {
+    // withheld copies: no stage is ever filled, the consumers' first waits
+    // run out and nothing is in flight when the CTAs leave
+    const int pend = sched.withhold ? beg : end;
+    for (int sl = beg; sl < pend; ++sl) {
       if (warp_failed(B)) break;
       // the next slot's entries load while this slot's copies are issued
       if (sl + 1 < end) load_slot(sched.items, sl + 1, nxt);
-      const SlotView v = view_of(cur, rank, sched.multicast != 0);
+      const SlotView v = view_of(cur, rank);
       const uint8_t* A = reinterpret_cast<const uint8_t*>(dig + v.it.a);
       const uint8_t* Bm = reinterpret_cast<const uint8_t*>(dig + v.it.b);
       const uint32_t a_lo = (uint32_t)(v.part * kABytes / max(v.nparts, 1));
@@ -305,7 +308,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (int u = 0; u < v.uses; ++u, ++g) {
         const int st = (int)(g % kStages);
         // every CTA this one writes to has released the stage
-        if (g >= (uint32_t)kStages && !warp_wait(&B->empty[st], ((g / kStages) - 1) & 1)) {
+        if (g >= (uint32_t)kStages && !warp_wait(&B->empty[st], ((g / kStages) - 1) & 1, wl)) {
           if (lane == 0) set_fail(B, ERR_EMPTY);
           ok = false;
           break;
@@ -345,7 +348,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     // cluster: the copies this CTA multicast have landed and the MMA commits
     // aimed at this CTA have arrived.
     for (uint32_t x = g > (uint32_t)kStages ? g - kStages : 0; x < g; ++x)
-      warp_wait(&B->empty[x % kStages], (x / kStages) & 1);
+      warp_wait(&B->empty[x % kStages], (x / kStages) & 1, wl);
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issue
     // descriptors of stage 0; stage st is st * kStageBytes / 16 further
@@ -359,16 +362,16 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int sl = beg; sl < end; ++sl) {
       if (warp_failed(B)) break;
       if (sl + 1 < end) load_slot(sched.items, sl + 1, nxt);
-      const SlotView v = view_of(cur, rank, sched.multicast != 0);
+      const SlotView v = view_of(cur, rank);
       // the epilogue has drained the previous tile's accumulators
-      if (v.nkb > 0 && li >= 1 && !warp_wait(&B->tempty, (li - 1) & 1)) {
+      if (v.nkb > 0 && li >= 1 && !warp_wait(&B->tempty, (li - 1) & 1, wl)) {
         if (lane == 0) set_fail(B, ERR_TEMPTY);
         break;
       }
       umma::fence_after_sync();
       bool ok = true;
       for (int u = 0; u < v.uses; ++u, ++g) {
-        if (!warp_wait(&B->full[st], ph)) {
+        if (!warp_wait(&B->full[st], ph, wl)) {
           if (lane == 0) set_fail(B, ERR_FULL);
           ok = false;
           break;
@@ -398,7 +401,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     // every MMA issued above has completed before TMEM is released
     if (lane == 0) umma::mma_commit(&B->done);
     __syncwarp();
-    warp_wait(&B->done, 0);
+    warp_wait(&B->done, 0, wl);
   } else {
     // ------------------------------------------------------------ epilogue
     // Work comes in units (TMEM lane quarter qq, 16-column chunk c).  Warps
@@ -456,7 +459,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         ecz = exp_of_pow2(base[o.cz]);
       }
       if (!helper) {
-        if (!warp_wait(&B->tfull, lc & 1)) {
+        if (!warp_wait(&B->tfull, lc & 1, wl)) {
           if (lane == 0) set_fail(B, ERR_TFULL);
           break;
         }
@@ -494,7 +497,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       };
       if (relay) {
         // hand both chunks over once the helpers are done with the previous ones
-        if (hc >= 1 && !warp_wait(&B->hempty, (hc - 1) & 1)) {
+        if (hc >= 1 && !warp_wait(&B->hempty, (hc - 1) & 1, wl)) {
           if (lane == 0) set_fail(B, ERR_HAND);
           break;
         }
@@ -506,7 +509,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         clear(hi[1], lo[1]);
         continue;
       }
-      if (helper && !warp_wait(&B->hfull, hc & 1)) {
+      if (helper && !warp_wait(&B->hfull, hc & 1, wl)) {
         if (lane == 0) set_fail(B, ERR_HAND);
         break;
       }

@@ -65,10 +65,16 @@ __global__ void ssf_weights_kernel(int64_t npts, int natoms, const int32_t* __re
                                    const double* __restrict__ dist_nearest,
                                    const double* __restrict__ rab_inv, int ld_rab,
                                    const double* __restrict__ dist, int ld,
-                                   double* __restrict__ weights) {
+                                   double* __restrict__ weights, int* __restrict__ status) {
   const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (p >= npts) return;
   const int ip = iparent[p];
+  if (ip < 0 || ip >= natoms) {
+    // a parent index outside the molecule: the point keeps its weight and
+    // the call reports the error (when the caller passed a status word)
+    if (status) atomicExch(status, 1);
+    return;
+  }
   const double cutoff = 0.5 * (1. - kSSFa) * dist_nearest[p];
   if (dist[(int64_t)ip * ld + p] < cutoff) return;
   const double parent = cell_product(ip, natoms, p, dist, ld, rab_inv, ld_rab);
@@ -88,14 +94,15 @@ __global__ void ssf_weights_kernel(int64_t npts, int natoms, const int32_t* __re
 void launch_ssf_weights(int64_t npts, int natoms, const double* x, const double* y,
                         const double* z, const int32_t* iparent, const double* dist_nearest,
                         const double* coords, const double* rab_inv, int ld_rab,
-                        double* dist_scr, int ld_dist, double* weights, cudaStream_t s) {
+                        double* dist_scr, int ld_dist, double* weights, int* status,
+                        cudaStream_t s) {
   if (npts == 0) return;
   const int threads = 256;
   dim3 g1((unsigned)((npts + threads - 1) / threads), (unsigned)std::min(natoms, 64));
   grid_to_center_kernel<<<g1, threads, 0, s>>>(npts, natoms, x, y, z, coords, dist_scr, ld_dist);
   dim3 g2((unsigned)((npts + threads - 1) / threads));
   ssf_weights_kernel<<<g2, threads, 0, s>>>(npts, natoms, iparent, dist_nearest, rab_inv, ld_rab,
-                                            dist_scr, ld_dist, weights);
+                                            dist_scr, ld_dist, weights, status);
   GB300_CUDA(cudaGetLastError());
 }
 

@@ -15,11 +15,12 @@
 //     points into several calls;
 //   * all calls share the one array: calls whose work overlaps on the GPU (two
 //     streams, two host threads) race and must be serialized by the caller;
-//   * the first call on a device looks up the array's device address
-//     (cudaGetSymbolAddress) with that device current; make that first call
-//     before any stream capture.
-#include <mutex>
-
+//   * every call looks up the array's device address (cudaGetSymbolAddress)
+//     on the current device, so the address stays right after a context
+//     reset; the first call on a device also loads this library's device
+//     code there and should come before any stream capture;
+//   * parent indices must lie in [0, natoms): a point whose parent does not
+//     keeps its weight (the call does not synchronize, so it cannot report it).
 #include "../host/device_api.hpp"
 #include "device_common.cuh"
 
@@ -30,24 +31,13 @@ namespace {
 constexpr int64_t kNoAllocScratchDoubles = int64_t(1) << 22;
 __device__ __align__(256) double g_ssf_scratch[kNoAllocScratchDoubles];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_addr_mutex;
-double* g_addr[kMaxDevices] = {};
-
-// Device address of g_ssf_scratch for the current device (looked up once).
+// Device address of g_ssf_scratch in the current device's context.
 double* scratch_address() {
-  int dev = 0;
-  GB300_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) throw error("device index out of range");
-  std::lock_guard<std::mutex> lock(g_addr_mutex);
-  if (!g_addr[dev]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_ssf_scratch);
-    if (e != cudaSuccess)
-      throw error(std::string("cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
-    g_addr[dev] = static_cast<double*>(p);
-  }
-  return g_addr[dev];
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_ssf_scratch);
+  if (e != cudaSuccess)
+    throw error(std::string("cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
+  return static_cast<double*>(p);
 }
 
 // rab_inv[a * natoms + b] = 1 / |R_a - R_b| (0 on the diagonal)
@@ -87,7 +77,7 @@ void ssf_weights_noalloc(int64_t npts, int natoms, const double* x, const double
   rab_inverse_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, s>>>(natoms, coords, rab_inv);
   GB300_CUDA(cudaGetLastError());
   launch_ssf_weights(npts, natoms, x, y, z, iparent, dist_nearest, coords, rab_inv, natoms, dist,
-                     (int)npts, weights, s);
+                     (int)npts, weights, nullptr, s);
 }
 
 }  // namespace gb300

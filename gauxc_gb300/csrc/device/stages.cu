@@ -36,7 +36,8 @@ void ssf_batched(int64_t npts, int natoms, const double* x, const double* y, con
   const int64_t bsz = std::max<int64_t>(1, std::min<int64_t>(npts, max_scr_doubles / natoms));
   DevBuf<double> dx(bsz), dy(bsz), dz(bsz), dw(bsz), ddn(bsz), dc(3 * natoms),
       drab((size_t)natoms * natoms), dscr((size_t)bsz * natoms);
-  DevBuf<int32_t> dip(bsz);
+  DevBuf<int32_t> dip(bsz), dstat(1);
+  GB300_CUDA(cudaMemsetAsync(dstat.p, 0, sizeof(int), s));
   GB300_CUDA(cudaMemcpyAsync(dc.p, coords, 3 * natoms * sizeof(double), cudaMemcpyHostToDevice, s));
   GB300_CUDA(cudaMemcpyAsync(drab.p, rab_inv.data(), rab_inv.size() * sizeof(double),
                              cudaMemcpyHostToDevice, s));
@@ -50,11 +51,14 @@ void ssf_batched(int64_t npts, int natoms, const double* x, const double* y, con
     GB300_CUDA(cudaMemcpyAsync(ddn.p, dn + b, nd, cudaMemcpyHostToDevice, s));
     GB300_CUDA(cudaMemcpyAsync(dip.p, ip + b, n * sizeof(int32_t), cudaMemcpyHostToDevice, s));
     launch_ssf_weights(n, natoms, dx.p, dy.p, dz.p, dip.p, ddn.p, dc.p, drab.p, natoms, dscr.p,
-                       (int)n, dw.p, s);
+                       (int)n, dw.p, dstat.p, s);
     GB300_CUDA(cudaMemcpyAsync(w + b, dw.p, nd, cudaMemcpyDeviceToHost, s));
     GB300_CUDA(cudaStreamSynchronize(s));
   }
+  int bad = 0;
+  GB300_CUDA(cudaMemcpy(&bad, dstat.p, sizeof(int), cudaMemcpyDeviceToHost));
   GB300_CUDA(cudaStreamDestroy(s));
+  if (bad) throw error("SSF weights: a parent atom index lies outside the molecule");
 }
 
 std::vector<double> rab_inverse(int natoms, const double* coords) {

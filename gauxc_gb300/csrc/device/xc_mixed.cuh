@@ -118,13 +118,19 @@ inline void oz_set_operands(OzItem& it, const PBDims& d, int64_t dig_off, bool v
 // Work list of one persistent GEMM launch on clusters of kCluster CTAs:
 // cluster c processes slots slot_off[c] .. slot_off[c + 1] - 1 in order; CTA
 // r of the cluster takes items[kCluster * slot + r] (pb < 0: none).
-// multicast = 0: every CTA loads its own A operand (no cluster multicast).
+// wait_ns bounds every pipeline wait of the launch (a wait that runs longer
+// records an error code and the CTAs leave).  withhold != 0 makes every
+// producer issue no copy at all, so that the first wait on a stage runs out
+// with nothing in flight: the check of the error path (the error status
+// reaches the host and the next call runs normally).
 constexpr int kCluster = 4;
+constexpr uint64_t kOzWaitNs = 1000000000ull;  // 1 s
 struct OzSchedule {
   const OzItem* items;
   const int* slot_off;
   int nclusters;
-  int multicast = 1;
+  uint64_t wait_ns = kOzWaitNs;
+  int withhold = 0;
 };
 
 void launch_collocation_masked(const ShellsDev& sh, const TasksDev& tk, const PBMaskDev& mk,

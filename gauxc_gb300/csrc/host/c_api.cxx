@@ -1,8 +1,11 @@
 // extern "C" layer: the reference C API for the device XC path
 // (src/c-api/*.cxx) plus the gauxc_gb300_* extensions.  Error behaviour
 // follows src/c-api/c_status.hpp:12-44: a call first resets the status
-// (freeing an old message), failures set code = 1 and a malloc'd message,
-// and exceptions never cross the C boundary.
+// (freeing an old message) and failures set code = 1 and a malloc'd message.
+// A caller that passes a null status gets the failure as a C++ exception
+// (gb300::error, a std::runtime_error), as the reference throws
+// GAUXC_GENERIC_EXCEPTION in that case; with a status, no exception crosses
+// the C boundary.
 #include <cstdlib>
 #include <cstring>
 #include <memory>
@@ -24,7 +27,7 @@ void status_init(GauXCStatus* st) {
 }
 
 void status_fail(GauXCStatus* st, const char* msg) {
-  if (!st) return;
+  if (!st) throw gb300::error(msg);
   st->code = 1;
   std::free(st->message);
   const size_t n = std::strlen(msg) + 1;
@@ -667,6 +670,24 @@ void gauxc_gb300_load_balancer_task_data(GauXCStatus* status, const GauXCLoadBal
   if (shell_list) std::memcpy(shell_list, t.shell_list.data(), t.shell_list.size() * sizeof(int32_t));
 }
 
+GauXCLoadBalancer gauxc_gb300_load_balancer_subset(GauXCStatus* status, const GauXCLoadBalancer lb,
+                                                   const int64_t* task_idx, size_t n) {
+  status_init(status);
+  GauXCLoadBalancer h{};
+  h.hdr.type = GauXC_Type_LoadBalancer;
+  if (!check(status, lb, GauXC_Type_LoadBalancer, "LoadBalancer")) return h;
+  if (n > 0 && !task_idx) {
+    status_fail(status, "task index array cannot be null");
+    return h;
+  }
+  guarded(status, [&] {
+    auto& L = deref<LoadBalancer>(lb.ptr);
+    std::vector<int64_t> idx(task_idx, task_idx + n);
+    h = make_handle<GauXCLoadBalancer>(GauXC_Type_LoadBalancer, load_balancer_subset(*L, idx));
+  });
+  return h;
+}
+
 bool gauxc_gb300_load_balancer_weights_modified(GauXCStatus* status, const GauXCLoadBalancer lb) {
   status_init(status);
   if (!check(status, lb, GauXC_Type_LoadBalancer, "LoadBalancer")) return false;
@@ -697,11 +718,12 @@ int gauxc_gb300_integrator_plan_stats(GauXCStatus* status, const GauXCIntegrator
   int n = 0;
   guarded(status, [&] {
     PlanStats s = integrator_plan_stats(*deref<XCIntegratorHandle>(integrator.ptr));
-    const double v[11] = {(double)s.ntasks, (double)s.npts, (double)s.npts_pad,
+    const double v[18] = {(double)s.ntasks, (double)s.npts, (double)s.npts_pad,
                           (double)s.nbatches, s.sum_npts_nbe, s.sum_npts_nbe2,
                           s.sum_pad_npts_nbe2, s.scratch_bytes, (double)s.gpu_launches,
-                          s.tensor_flops_x, s.tensor_flops_v};
-    for (; n < 11 && n < nmax; ++n) out[n] = v[n];
+                          s.tensor_flops_x, s.tensor_flops_v, s.kbytes[0], s.kbytes[1],
+                          s.kbytes[2], s.kbytes[3], s.kbytes[4], s.kbytes[5], s.kbytes[6]};
+    for (; n < 18 && n < nmax; ++n) out[n] = v[n];
   });
   return n;
 }
@@ -711,6 +733,16 @@ void gauxc_gb300_integrator_set_profiling(GauXCStatus* status, const GauXCIntegr
   status_init(status);
   if (!check(status, integrator, GauXC_Type_Integrator, "Integrator")) return;
   integrator_set_profiling(*deref<XCIntegratorHandle>(integrator.ptr), on);
+}
+
+void gauxc_gb300_integrator_set_pipeline_check(GauXCStatus* status,
+                                               const GauXCIntegrator integrator, double wait_ms,
+                                               bool withhold) {
+  status_init(status);
+  if (!check(status, integrator, GauXC_Type_Integrator, "Integrator")) return;
+  guarded(status, [&] {
+    integrator_set_pipeline_check(*deref<XCIntegratorHandle>(integrator.ptr), wait_ms, withhold);
+  });
 }
 
 int gauxc_gb300_integrator_kernel_times(GauXCStatus* status, const GauXCIntegrator integrator,

@@ -126,6 +126,12 @@ std::shared_ptr<LoadBalancer> make_load_balancer(
     std::shared_ptr<const Molecule> mol, std::shared_ptr<const MolGrid> mg,
     std::shared_ptr<const BasisSet> basis, bool device);
 
+// A load balancer over tasks `idx` of `lb` (in that order, each index in
+// range): same molecule, basis, grid and runtime, copies of the tasks with
+// their current weights and the weights-modified state.
+std::shared_ptr<LoadBalancer> load_balancer_subset(const LoadBalancer& lb,
+                                                   const std::vector<int64_t>& idx);
+
 // cube/sphere test (include/gauxc/util/geometry.hpp:36-49)
 inline bool cube_sphere_intersect(const double* lo, const double* up,
                                   const double* c, double rad) {

@@ -30,6 +30,10 @@ struct PlanStats {
   double scratch_bytes = 0.;
   int64_t gpu_launches = 0;
   double tensor_flops_x = 0., tensor_flops_v = 0.;  // BF16 MMA flops per call (mixed path)
+  // Algorithmic bytes per call of each kernel class (collocation, density,
+  // zmat / Z digits, vxc, other, phi digits, P digits): every operand read
+  // once and every result written once, at the sizes the plan runs
+  double kbytes[7] = {0, 0, 0, 0, 0, 0, 0};
 };
 
 // Tunable parameters of the tensor-core plan (point blocks).
@@ -52,6 +56,10 @@ struct XCIntegratorHandle {
   double last_exc = 0., last_nel = 0.;
   bool profiling = false;
   PlanParams params;
+  // bound of the tensor-core pipeline waits (ns) and the error-path check
+  // (integrator_set_pipeline_check)
+  uint64_t wait_ns = 1000000000ull;
+  bool withhold = false;
 };
 
 // eval_exc_vxc for RKS; VXC may be null (EXC only).  Throws gb300::error.
@@ -65,6 +73,11 @@ PlanStats integrator_plan_stats(XCIntegratorHandle& h);
 // zmat, vxc, other): {ms, launches} pairs of the last call.
 void integrator_set_profiling(XCIntegratorHandle& h, bool on);
 std::vector<double> integrator_kernel_times(const XCIntegratorHandle& h);
+// Bound of every tensor-core pipeline wait of the following calls, and the
+// check of their error path: with withhold set, the GEMM producers issue no
+// copy, each consumer's first wait runs out after wait_ms and the call fails
+// with the pipeline error; the context stays usable.
+void integrator_set_pipeline_check(XCIntegratorHandle& h, double wait_ms, bool withhold);
 // Sets the tensor-core plan parameters; the plan is rebuilt on the next call.
 void integrator_set_plan_params(XCIntegratorHandle& h, const PlanParams& p);
 // Times one call for each candidate plan (point-block sizes x merge weights)

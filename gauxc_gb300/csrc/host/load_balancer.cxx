@@ -131,4 +131,23 @@ std::shared_ptr<LoadBalancer> make_load_balancer(std::shared_ptr<const Molecule>
   return lb;
 }
 
+std::shared_ptr<LoadBalancer> load_balancer_subset(const LoadBalancer& lb,
+                                                   const std::vector<int64_t>& idx) {
+  auto sub = std::make_shared<LoadBalancer>();
+  sub->rt = lb.rt;
+  sub->mol = lb.mol;
+  sub->basis = lb.basis;
+  sub->molgrid = lb.molgrid;
+  sub->meta = lb.meta;
+  sub->device_screening = lb.device_screening;
+  sub->weights_modified = lb.weights_modified;
+  sub->tasks.reserve(idx.size());
+  for (int64_t i : idx) {
+    if (i < 0 || i >= (int64_t)lb.tasks.size()) throw error("task index out of range");
+    sub->tasks.push_back(lb.tasks[i]);
+  }
+  sub->generation = lb.generation + 1;
+  return sub;
+}
+
 }  // namespace gb300

@@ -247,6 +247,13 @@ void gauxc_gb300_load_balancer_task_data(GauXCStatus* status, const GauXCLoadBal
                                          size_t i, double* points, double* weights,
                                          int32_t* shell_list);
 bool gauxc_gb300_load_balancer_weights_modified(GauXCStatus* status, const GauXCLoadBalancer lb);
+/* A new load balancer over the tasks task_idx[0..n) of lb (in that order):
+   same molecule, basis, grid and runtime environment, copies of the tasks with
+   their current weights and weights-modified state.  Used to evaluate a
+   sample of a large system's tasks (parity checks and CPU timing samples).
+   No counterpart in the reference. */
+GauXCLoadBalancer gauxc_gb300_load_balancer_subset(GauXCStatus* status, const GauXCLoadBalancer lb,
+                                                   const int64_t* task_idx, size_t n);
 
 /* N_el (integral of the total density) of the last eval_exc_vxc call. */
 double gauxc_gb300_integrator_last_nel(GauXCStatus* status, const GauXCIntegrator integrator);
@@ -255,7 +262,10 @@ int gauxc_gb300_integrator_timings(GauXCStatus* status, const GauXCIntegrator in
                                    double* out, int nmax);
 /* Plan statistics: {ntasks, npts, npts_pad, nbatches, sum npts*nbe, sum npts*nbe^2,
    sum npts_pad*nbe_pad^2, scratch bytes, kernel launches of the last call,
-   BF16 tensor FLOPs per call of the density and of the VXC GEMMs (mixed path)}. */
+   BF16 tensor FLOPs per call of the density and of the VXC GEMMs (mixed path),
+   algorithmic bytes per call of the kernel classes collocation, density,
+   zmat (Z digits), vxc, other, phi digits, P digits (each operand read once,
+   each result written once)}; returns the count written (at most 18). */
 int gauxc_gb300_integrator_plan_stats(GauXCStatus* status, const GauXCIntegrator integrator,
                                       double* out, int nmax);
 
@@ -268,6 +278,16 @@ void gauxc_gb300_integrator_set_profiling(GauXCStatus* status, const GauXCIntegr
    of the last call (at most nmax values); returns the count written. */
 int gauxc_gb300_integrator_kernel_times(GauXCStatus* status, const GauXCIntegrator integrator,
                                         double* out, int nmax);
+/* Bound (ms, default 1000) of every wait of the tensor-core pipeline in the
+   following calls of a "GB300-Mixed" integrator, and the check of its error
+   path: with withhold set, the GEMM producers issue no copy at all, the first
+   wait of each consumer runs out after wait_ms with nothing in flight, and the
+   call fails with "a tensor-core pipeline wait expired"; the CUDA context stays
+   usable and a later call with withhold cleared runs normally.  No counterpart
+   in the reference (its device integrator has no bounded waits). */
+void gauxc_gb300_integrator_set_pipeline_check(GauXCStatus* status,
+                                               const GauXCIntegrator integrator, double wait_ms,
+                                               bool withhold);
 /* Measured FP64 FMA throughput of the current device in TFLOP/s (about 50 ms probe). */
 double gauxc_gb300_measure_fp64_peak(GauXCStatus* status);
 /* Page-lock caller host memory in place (P / VXC buffers reused every SCF
@@ -301,8 +321,11 @@ void gauxc_gb300_ssf_weights(GauXCStatus* status, int64_t npts, int32_t natoms,
    inside the library, kept by every GPU that loads it until exit:
    natoms*npts + natoms*natoms must not exceed 4194304 (larger requests are
    rejected; split the points).  All calls share that array, so calls that
-   overlap on the GPU race; the first call on a device looks the array up and
-   should come before any stream capture.  Nothing is allocated or freed. */
+   overlap on the GPU race.  Each call looks the array's address up on the
+   current device; the first call on a device also loads the library's device
+   code there and should come before any stream capture.  A point whose parent
+   index lies outside [0, natoms) keeps its weight.  Nothing is allocated or
+   freed. */
 void gauxc_gb300_ssf_weights_noalloc(GauXCStatus* status, int64_t npts, int32_t natoms,
                                      const double* x, const double* y, const double* z,
                                      const int32_t* iparent, const double* dist_nearest,

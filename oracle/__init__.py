@@ -30,18 +30,48 @@ def build():
     if os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(src):
         return LIB
     tmp = LIB + ".tmp"
-    subprocess.run(["g++", "-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared", src, "-o", tmp],
-                   check=True)
+    subprocess.run(["g++", "-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared", src, "-o", tmp,
+                    "-ldl"], check=True)
     os.replace(tmp, LIB)
     return LIB
 
 
+def blas_library():
+    """Path of the OpenBLAS that scipy bundles (the only CPU BLAS on these
+    machines), or None."""
+    import glob
+    try:
+        import scipy
+    except ImportError:
+        return None
+    base = os.path.dirname(os.path.dirname(os.path.abspath(scipy.__file__)))
+    for pat in ("scipy.libs/libscipy_openblas*.so*", "scipy/.libs/libscipy_openblas*.so*",
+                "scipy.libs/libopenblas*.so*"):
+        hits = sorted(glob.glob(os.path.join(base, pat)))
+        if hits:
+            return hits[0]
+    return None
+
+
 def lib():
+    """The oracle library; its contractions use scipy's OpenBLAS when present."""
     global _lib
     if _lib is None:
         build()
-        _lib = ctypes.CDLL(LIB)
+        L = ctypes.CDLL(LIB)
+        L.oracle_use_blas.restype = ctypes.c_int
+        L.oracle_use_blas.argtypes = [ctypes.c_char_p]
+        L.oracle_blas_active.restype = ctypes.c_int
+        path = blas_library()
+        if path:
+            L.oracle_use_blas(path.encode())
+        _lib = L
     return _lib
+
+
+def blas_active():
+    """True when the contractions run on a BLAS (dgemm / dsyr2k)."""
+    return bool(lib().oracle_blas_active())
 
 
 def _p(a, ct=ctypes.c_double):

@@ -22,6 +22,11 @@
 // papers; vrho / vsigma come from forward-mode dual numbers, independent of
 // the hand-derived derivatives used on the device.  Density thresholds equal
 // the device ones (1e-15; 1e-12 for PBE correlation).
+// The two contractions use a BLAS when oracle_use_blas() found one, as the
+// reference host driver does (blas::gemm for X, blas::syr2k for V:
+// reference_local_host_work_driver.cxx:143, :1688), one BLAS thread per
+// OpenMP task thread; otherwise a plain blocked loop.
+#include <dlfcn.h>
 #include <omp.h>
 
 #include <algorithm>
@@ -288,9 +293,45 @@ void gemm(int m, int n, int k, double alpha, const double* A, int lda, const dou
   }
 }
 
+// Fortran BLAS entry points, found at run time (oracle_use_blas).
+typedef void (*dgemm_fn)(const char*, const char*, const int*, const int*, const int*,
+                         const double*, const double*, const int*, const double*, const int*,
+                         const double*, double*, const int*);
+typedef void (*dsyr2k_fn)(const char*, const char*, const int*, const int*, const double*,
+                          const double*, const int*, const double*, const int*, const double*,
+                          double*, const int*);
+dgemm_fn g_dgemm = nullptr;
+dsyr2k_fn g_dsyr2k = nullptr;
+
 }  // namespace
 
 extern "C" {
+
+// Loads a BLAS shared library (path) and uses its dgemm / dsyr2k for the
+// contractions from now on (names with or without the "scipy_" prefix of
+// scipy's bundled OpenBLAS).  Returns 1 on success, 0 when the library or a
+// symbol is missing (the loop contractions stay in use).
+int oracle_use_blas(const char* path) {
+  void* h = dlopen(path, RTLD_NOW | RTLD_LOCAL);
+  if (!h) return 0;
+  auto sym = [&](const char* a, const char* b) {
+    void* p = dlsym(h, a);
+    return p ? p : dlsym(h, b);
+  };
+  auto gm = reinterpret_cast<dgemm_fn>(sym("scipy_dgemm_", "dgemm_"));
+  auto s2 = reinterpret_cast<dsyr2k_fn>(sym("scipy_dsyr2k_", "dsyr2k_"));
+  if (!gm || !s2) return 0;
+  // one BLAS thread: the oracle runs its tasks on OpenMP threads
+  typedef void (*setn_fn)(int);
+  if (auto sn = reinterpret_cast<setn_fn>(sym("scipy_openblas_set_num_threads",
+                                              "openblas_set_num_threads")))
+    sn(1);
+  g_dgemm = gm;
+  g_dsyr2k = s2;
+  return 1;
+}
+
+int oracle_blas_active() { return g_dgemm != nullptr; }
 
 // --------------------------------------------------------------- shells
 void oracle_normalize_shell(int l, int nprim, const double* alpha, double* coeff) {
@@ -435,7 +476,13 @@ void oracle_eval_exc_vxc(int nshells_basis, const int32_t* l, const int32_t* pur
         for (int i = 0; i < nbe; ++i) Ps[(size_t)j * nbe + i] = P[(size_t)bf[j] * nbf + bf[i]];
       // X = 2 * P_sub * B   (nbe x npts)
       X.resize(ne);
-      gemm(nbe, npts, nbe, 2.0, Ps.data(), nbe, f.data(), nbe, false, X.data(), nbe);
+      if (g_dgemm) {
+        const double two = 2.0, zero = 0.0;
+        g_dgemm("N", "N", &nbe, &npts, &nbe, &two, Ps.data(), &nbe, f.data(), &nbe, &zero,
+                X.data(), &nbe);
+      } else {
+        gemm(nbe, npts, nbe, 2.0, Ps.data(), nbe, f.data(), nbe, false, X.data(), nbe);
+      }
       rho.resize(npts);
       gxv.assign(npts, 0.);
       gyv.assign(npts, 0.);
@@ -483,10 +530,17 @@ void oracle_eval_exc_vxc(int nshells_basis, const int32_t* l, const int32_t* pur
         }
       // V = B Z^T + Z B^T (nbe x nbe), lower triangle scattered atomically
       V.resize((size_t)nbe * nbe);
-      gemm(nbe, nbe, npts, 1.0, f.data(), nbe, Zm.data(), nbe, true, V.data(), nbe);
+      if (g_dsyr2k) {
+        const double one = 1.0, zero = 0.0;
+        g_dsyr2k("L", "N", &nbe, &npts, &one, f.data(), &nbe, Zm.data(), &nbe, &zero, V.data(),
+                 &nbe);
+      } else {
+        gemm(nbe, nbe, npts, 1.0, f.data(), nbe, Zm.data(), nbe, true, V.data(), nbe);
+      }
       for (int j = 0; j < nbe; ++j)
         for (int i = j; i < nbe; ++i) {
-          const double v = V[(size_t)j * nbe + i] + V[(size_t)i * nbe + j];
+          const double v = g_dsyr2k ? V[(size_t)j * nbe + i]
+                                    : V[(size_t)j * nbe + i] + V[(size_t)i * nbe + j];
           const int gi = bf[i], gj = bf[j];
           // lower triangle of the global matrix
           const int r_ = std::max(gi, gj), c_ = std::min(gi, gj);

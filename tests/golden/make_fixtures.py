@@ -1,9 +1,9 @@
 """Extract small ``.npz`` fixtures from the reference's HDF5 golden files.
 
-Run in a container that has the reference checkout (read-only) at
-``$GAUXC_REF`` (default ``/root/reference``)::
+Run where the reference checkout (read-only) is available, with its root in
+``$GAUXC_REF``::
 
-    python tests/golden/make_fixtures.py
+    GAUXC_REF=<reference checkout> python tests/golden/make_fixtures.py
 
 The GPU test machines never see the reference tree; they only read the
 committed ``.npz`` files this script writes next to itself.
@@ -34,8 +34,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 from h5lite import H5File  # noqa: E402
 
-REF = os.environ.get("GAUXC_REF", "/root/reference")
-DATA = os.path.join(REF, "tests", "ref_data")
+REF = os.environ.get("GAUXC_REF")
+DATA = os.path.join(REF, "tests", "ref_data") if REF else None
 POINT_STRIDE = 7
 
 
@@ -193,6 +193,8 @@ def g94_case():
 
 
 if __name__ == "__main__":
+    if not REF or not os.path.isdir(DATA):
+        sys.exit("set GAUXC_REF to the reference checkout (its tests/ref_data holds the HDF5 files)")
     xc_case("benzene_svwn5_cc-pvdz_ufg_ssf.hdf5", "benzene_svwn5.npz")
     xc_case("benzene_svwn5_cc-pvdz_ufg_ssf_treutler_prune.hdf5", "benzene_svwn5_treutler.npz")
     xc_case("benzene_pbe0_cc-pvdz_ufg_ssf.hdf5", "benzene_pbe0.npz")

@@ -98,3 +98,51 @@ def test_device_paths_fail_loudly_without_gpu(g):
         mw.modify_weights(lb)
     with pytest.raises(GauXCError, match="no CUDA device"):
         g.collocation(basis, np.zeros((4, 3)), [0, 1])
+
+
+def test_pipeline_check_arguments(g):
+    from gauxc_gb300 import workloads as W
+    from gauxc_gb300._capi import GauXCError
+    s = W.config(0)["systems"][0]
+    mol, basis, mg, lb = W.build_system(s, device=False)
+    integ = g.XCIntegratorFactory(g.ExecutionSpace.Device, "Replicated", "Default",
+                                  "GB300-Mixed", "Default").get_instance(
+                                      g.functional_type(s["functional"]), lb)
+    integ.set_pipeline_check(wait_ms=2.0, withhold=True)
+    integ.set_pipeline_check()
+    for bad in (0.0, -1.0, 1e9):
+        with pytest.raises(GauXCError, match="pipeline wait bound"):
+            integ.set_pipeline_check(wait_ms=bad)
+
+
+def test_load_balancer_subset_copies_tasks(g):
+    from gauxc_gb300 import workloads as W
+    from gauxc_gb300._capi import GauXCError
+    s = W.config(5)["systems"][0]
+    mol, basis, mg, lb = W.build_system(s, device=False)
+    n = lb.ntasks()
+    idx = [n - 1, 0, n // 2]
+    sub = lb.subset(idx)
+    assert sub.ntasks() == 3 and sub.weights_modified() == lb.weights_modified()
+    for k, i in enumerate(idx):
+        a, b = lb.task(i), sub.task(k)
+        assert a["iParent"] == b["iParent"] and a["nbe"] == b["nbe"]
+        assert np.array_equal(a["points"], b["points"])
+        assert np.array_equal(a["weights"], b["weights"])
+        assert np.array_equal(a["shell_list"], b["shell_list"])
+    assert lb.subset([]).ntasks() == 0
+    with pytest.raises(GauXCError, match="out of range"):
+        lb.subset([n])
+
+
+def test_null_status_raises_like_the_reference(g):
+    """With a null GauXCStatus* a failure is thrown as a C++ exception
+    (src/c-api/c_status.hpp:31-44); the compiled C++ walk-through in
+    test_native_clients.py catches it.  From ctypes only the success path can
+    pass a null status: it must return normally."""
+    L = g.lib()
+    m = L.gauxc_molecule_new(None)
+    assert m.ptr
+    assert L.gauxc_molecule_natoms(None, m) == 0
+    L.gauxc_molecule_delete(None, ctypes.byref(m))
+    assert not m.ptr

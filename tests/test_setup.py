@@ -137,6 +137,29 @@ def test_task_list_invariants_and_golden_metadata(g):
     assert keys == sorted(keys) and len(set(keys)) == len(keys)
 
 
+def test_task_list_keyed_against_golden(g):
+    """Keyed comparison with the reference task list of the same system: the
+    (iParent, shell_list) keys both lists hold, and the points under them.
+    The batcher here is this project's own (IntegratorXX's is not in the
+    reference tree), so batch boundaries, and with them the per-key point
+    counts, differ; the shared keys hold most of the reference's points.
+    Measured: 253 of the reference's 664 keys are shared, holding 89.3 % of
+    its points (88.6 % of ours); no shared key has the same point count."""
+    gt = golden("benzene_tasks.npz")
+    d, mol, basis, mg, lb = benzene_system(g, "benzene_svwn5.npz", device=False)
+    ours = {(t["iParent"], tuple(int(x) for x in t["shell_list"])): t["npts"]
+            for t in lb.get_tasks()}
+    theirs = {}
+    for i in range(len(gt["npts"])):
+        sl = gt["shell_list"][gt["shell_off"][i]:gt["shell_off"][i + 1]]
+        theirs[(int(gt["iparent"][i]), tuple(int(x) for x in sl))] = int(gt["npts"][i])
+    common = set(ours) & set(theirs)
+    frac_keys = len(common) / len(theirs)
+    frac_pts = sum(theirs[k] for k in common) / sum(theirs.values())
+    assert len(theirs) == 664 and sum(theirs.values()) == 12 * 99 * 590
+    assert frac_keys >= 0.38 and frac_pts >= 0.89
+
+
 def test_empty_and_far_batches_are_dropped(g):
     """A shell far from the atom screens out every batch: no tasks at all."""
     mol = g.Molecule([(1, 0.0, 0.0, 0.0)])
