@@ -15,6 +15,7 @@
 // per-point loops read consecutive addresses across a warp.
 #include "device_common.cuh"
 
+#include <algorithm>
 #include <cfloat>
 
 namespace gb300 {
@@ -89,7 +90,203 @@ __global__ void ssf_weights_kernel(int64_t npts, int natoms, const int32_t* __re
   }
   weights[p] *= parent / sum;
 }
+// ---------------------------------------------------------------- screened kernel
+// Same weights, far fewer cell-product factors.  A warp takes 32 consecutive
+// points (a chunk; the points of one task are close together) and
+//   * sorts the atoms by their distance d_B to the centre of the chunk's
+//     bounding box (bitonic sort of (d_B, B) keys in shared memory), h being
+//     the chunk's radius, so that every point has r_B in [d_B - h, d_B + h];
+//   * drops, for the whole chunk, every atom A that one of the four atoms
+//     nearest to the centre kills at every point:
+//     ((d_A - h) - (d_B + h)) / R_AB >= a gives s(mu_AB) = 0, so P_A = 0;
+//   * evaluates each remaining cell product over the atoms in distance
+//     order: the nearest atoms (the likely zero factors) come first, and the
+//     loop ends at the first atom with d_B - h >= r_A (1 + a) / (1 - a):
+//     from there on R_AB <= r_A + r_B gives mu_AB <= -a, a factor of exactly
+//     1 for every later atom.
+// The cell products follow the reference's rules: a zero factor ends the
+// product, and so does a product at or below 1e-13 (kept as it is).  Only
+// the order of the factors differs from cuda_ssf_1d.cu (nearest first instead
+// of atom index order); atoms dropped for the chunk contribute exactly 0.
+// Margins of 1e-9 on mu and of 1e-12 relative / 1e-10 bohr on h keep every
+// bound valid under FP64 rounding.
+constexpr int kSSFWarps = 4;
+constexpr double kSSFFar = (1. + kSSFa) / (1. - kSSFa);
+
+__device__ __forceinline__ double warp_min(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Cell product P_A at point p over the atoms in the chunk's distance order.
+__device__ __forceinline__ double cell_sorted(int A, int natoms, int64_t p, double h,
+                                              const uint64_t* __restrict__ keys,
+                                              const double* __restrict__ dist, int ld,
+                                              const double* __restrict__ rab_inv, int ld_rab) {
+  const double rA = dist[(int64_t)A * ld + p];
+  const double* rinv = rab_inv + (int64_t)A * ld_rab;
+  // atoms with d_B >= lim have r_B >= kSSFFar r_A (1 + 1e-9): factor 1
+  const double lim = kSSFFar * rA * (1. + 1e-9) + h;
+  double ps = 1.;
+  for (int k = 0; k < natoms; ++k) {
+    const uint64_t key = keys[k];
+    if ((double)__uint_as_float((unsigned)(key >> 32)) >= lim) break;
+    const int B = (int)(key & 0xFFFFu);
+    if (B == A) continue;
+    const double mu = (rA - dist[(int64_t)B * ld + p]) * rinv[B];
+    if (mu >= kSSFa) return 0.;
+    if (mu > -kSSFa) {
+      ps *= ssf_s(mu);
+      if (ps <= kSSFTol) break;
+    }
+  }
+  return ps;
+}
+
+__global__ void __launch_bounds__(kSSFWarps * 32)
+    ssf_screened_kernel(int64_t npts, int natoms, int nsort, const double* __restrict__ x,
+                        const double* __restrict__ y, const double* __restrict__ z,
+                        const int32_t* __restrict__ iparent,
+                        const double* __restrict__ dist_nearest,
+                        const double* __restrict__ coords, const double* __restrict__ rab_inv,
+                        int ld_rab, const double* __restrict__ dist, int ld,
+                        double* __restrict__ weights, int* __restrict__ status) {
+  extern __shared__ uint64_t ssf_smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // per warp: nsort sort keys, then up to nsort candidate atoms (uint16)
+  uint64_t* keys = ssf_smem + (size_t)warp * (nsort + nsort / 4);
+  uint16_t* cand = reinterpret_cast<uint16_t*>(keys + nsort);
+  const int64_t p0 = ((int64_t)blockIdx.x * kSSFWarps + warp) * 32;
+  if (p0 >= npts) return;  // the whole warp
+  const int64_t p = p0 + lane;
+  const bool act = p < npts;
+  const int64_t pq = act ? p : p0;
+  const double px = x[pq], py = y[pq], pz = z[pq];
+  const double cx = 0.5 * (warp_min(px) + warp_max(px));
+  const double cy = 0.5 * (warp_min(py) + warp_max(py));
+  const double cz = 0.5 * (warp_min(pz) + warp_max(pz));
+  double h = sqrt((px - cx) * (px - cx) + (py - cy) * (py - cy) + (pz - cz) * (pz - cz));
+  h = warp_max(h) * (1. + 1e-12) + 1e-10;
+
+  // ---- atoms in distance order (keys: d_B as float rounded down, atom index)
+  for (int b = lane; b < nsort; b += 32) {
+    uint64_t k = ~0ull;
+    if (b < natoms) {
+      const double dx = cx - coords[3 * b], dy = cy - coords[3 * b + 1], dz = cz - coords[3 * b + 2];
+      const float df = __double2float_rd(sqrt(dx * dx + dy * dy + dz * dz));
+      k = ((uint64_t)__float_as_uint(df) << 32) | (uint64_t)b;
+    }
+    keys[b] = k;
+  }
+  __syncwarp();
+  for (int kk = 2; kk <= nsort; kk <<= 1)
+    for (int j = kk >> 1; j > 0; j >>= 1) {
+      for (int i = lane; i < nsort; i += 32) {
+        const int ixj = i ^ j;
+        if (ixj > i) {
+          const uint64_t u = keys[i], v = keys[ixj];
+          if ((u > v) == ((i & kk) == 0)) {
+            keys[i] = v;
+            keys[ixj] = u;
+          }
+        }
+      }
+      __syncwarp();
+    }
+
+  // ---- atoms not killed at every point of the chunk by one of the four nearest
+  int kb[4];
+  double kd[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    kb[q] = q < natoms ? (int)(keys[q] & 0xFFFFu) : -1;
+    if (kb[q] >= 0) {
+      const double dx = cx - coords[3 * kb[q]], dy = cy - coords[3 * kb[q] + 1],
+                   dz = cz - coords[3 * kb[q] + 2];
+      kd[q] = sqrt(dx * dx + dy * dy + dz * dz) + h;  // upper bound of r_B
+    }
+  }
+  int ncand = 0;
+  for (int a0 = 0; a0 < natoms; a0 += 32) {
+    const int A = a0 + lane;
+    bool keep = A < natoms;
+    if (keep) {
+      const double dx = cx - coords[3 * A], dy = cy - coords[3 * A + 1], dz = cz - coords[3 * A + 2];
+      const double dlo = sqrt(dx * dx + dy * dy + dz * dz) - h;  // lower bound of r_A
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (kb[q] >= 0 && kb[q] != A &&
+            (dlo - kd[q]) * rab_inv[(int64_t)A * ld_rab + kb[q]] >= kSSFa + 1e-9)
+          keep = false;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (keep) cand[ncand + __popc(m & ((1u << lane) - 1))] = (uint16_t)A;
+    ncand += __popc(m);
+  }
+  __syncwarp();
+  if (!act) return;
+
+  // ---- this lane's point (reference rules, cuda_ssf_1d.cu:61-128)
+  const int ip = iparent[p];
+  if (ip < 0 || ip >= natoms) {
+    if (status) atomicExch(status, 1);
+    return;
+  }
+  const double cutoff = 0.5 * (1. - kSSFa) * dist_nearest[p];
+  if (dist[(int64_t)ip * ld + p] < cutoff) return;
+  const double parent = cell_sorted(ip, natoms, p, h, keys, dist, ld, rab_inv, ld_rab);
+  if (parent < DBL_EPSILON) {
+    weights[p] = 0.;
+    return;
+  }
+  double sum = parent;
+  for (int c = 0; c < ncand; ++c) {
+    const int A = cand[c];
+    if (A == ip) continue;
+    sum += cell_sorted(A, natoms, p, h, keys, dist, ld, rab_inv, ld_rab);
+  }
+  weights[p] *= parent / sum;
+}
+
 }  // namespace
+
+void launch_ssf_weights_screened(int64_t npts, int natoms, const double* x, const double* y,
+                                 const double* z, const int32_t* iparent,
+                                 const double* dist_nearest, const double* coords,
+                                 const double* rab_inv, int ld_rab, double* dist_scr, int ld_dist,
+                                 double* weights, int* status, cudaStream_t s) {
+  if (npts == 0) return;
+  if (natoms > kSSFScreenedMaxAtoms) {
+    launch_ssf_weights(npts, natoms, x, y, z, iparent, dist_nearest, coords, rab_inv, ld_rab,
+                       dist_scr, ld_dist, weights, status, s);
+    return;
+  }
+  const int threads = 256;
+  dim3 g1((unsigned)((npts + threads - 1) / threads), (unsigned)std::min(natoms, 64));
+  grid_to_center_kernel<<<g1, threads, 0, s>>>(npts, natoms, x, y, z, coords, dist_scr, ld_dist);
+  int nsort = 32;
+  while (nsort < natoms) nsort <<= 1;
+  const size_t smem = (size_t)kSSFWarps * (nsort + nsort / 4) * sizeof(uint64_t);
+  static bool attr = false;
+  if (!attr) {
+    GB300_CUDA(cudaFuncSetAttribute(ssf_screened_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)((size_t)kSSFWarps * (kSSFScreenedMaxAtoms + kSSFScreenedMaxAtoms / 4) *
+                                          sizeof(uint64_t))));
+    attr = true;
+  }
+  const int64_t chunks = (npts + 31) / 32;
+  const unsigned blocks = (unsigned)((chunks + kSSFWarps - 1) / kSSFWarps);
+  ssf_screened_kernel<<<blocks, kSSFWarps * 32, smem, s>>>(npts, natoms, nsort, x, y, z, iparent,
+                                                           dist_nearest, coords, rab_inv, ld_rab,
+                                                           dist_scr, ld_dist, weights, status);
+  GB300_CUDA(cudaGetLastError());
+}
 
 void launch_ssf_weights(int64_t npts, int natoms, const double* x, const double* y,
                         const double* z, const int32_t* iparent, const double* dist_nearest,

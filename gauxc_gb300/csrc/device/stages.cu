@@ -50,8 +50,8 @@ void ssf_batched(int64_t npts, int natoms, const double* x, const double* y, con
     GB300_CUDA(cudaMemcpyAsync(dw.p, w + b, nd, cudaMemcpyHostToDevice, s));
     GB300_CUDA(cudaMemcpyAsync(ddn.p, dn + b, nd, cudaMemcpyHostToDevice, s));
     GB300_CUDA(cudaMemcpyAsync(dip.p, ip + b, n * sizeof(int32_t), cudaMemcpyHostToDevice, s));
-    launch_ssf_weights(n, natoms, dx.p, dy.p, dz.p, dip.p, ddn.p, dc.p, drab.p, natoms, dscr.p,
-                       (int)n, dw.p, dstat.p, s);
+    launch_ssf_weights_screened(n, natoms, dx.p, dy.p, dz.p, dip.p, ddn.p, dc.p, drab.p, natoms,
+                                dscr.p, (int)n, dw.p, dstat.p, s);
     GB300_CUDA(cudaMemcpyAsync(w + b, dw.p, nd, cudaMemcpyDeviceToHost, s));
     GB300_CUDA(cudaStreamSynchronize(s));
   }

@@ -105,6 +105,12 @@ void host_unregister(void* p);
 double tensor_core_selftest(int n, int k);
 void set_device(int dev);
 
+// Collision bitset of task boxes (6 doubles each: lo xyz, up xyz) against the
+// shells' cutoff spheres on the device: bit s % 32 of bits[i * nwords + s / 32]
+// is set when shell s survives the cube/sphere test for box i.
+void screen_boxes_device(const std::vector<double>& boxes, const BasisSet& bs,
+                         std::vector<uint32_t>& bits, int& nwords);
+
 // SSF weights on the device for every task of the load balancer.
 void molecular_weights_ssf_device(LoadBalancer& lb, RuntimeEnv& rt);
 

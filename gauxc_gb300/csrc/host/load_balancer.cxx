@@ -9,8 +9,11 @@
 //   * tasks are sorted by (iParent, shell_list) and tasks with identical
 //     (iParent, shell_list) are merged by concatenating their points.
 // Single-process build: every task is local (the reference's rank assignment
-// by XCTask::cost is the identity for one rank).
+// by XCTask::cost is the identity for one rank).  The Device load balancer
+// screens the candidate boxes on the GPU (screening.cu) and gives the same
+// task list.
 #include "core.hpp"
+#include "device_api.hpp"
 
 #include <algorithm>
 #include <atomic>
@@ -50,11 +53,34 @@ std::shared_ptr<LoadBalancer> make_load_balancer(std::shared_ptr<const Molecule>
   lb->meta = std::make_shared<MolMeta>(*mol);
   lb->device_screening = device;
 
-  // Task candidates of every atom, atoms spread over host threads; the lists
-  // are joined in atom order, so the result does not depend on the threads.
+  // Task candidates of every atom (points, weights, the batch's bounding box),
+  // atoms spread over host threads; the lists are joined in atom order, so
+  // the result does not depend on the threads.  The host screens each box as
+  // it goes; the Device load balancer screens all boxes in one kernel.
   const size_t nat = mol->size();
   std::vector<std::vector<XCTask>> per_atom(nat);
-  auto atom_tasks = [&](size_t iat) {
+  std::vector<std::vector<double>> per_atom_box(nat);
+  auto parallel_atoms = [&](auto&& fn) {
+    const size_t nth = std::min<size_t>(nat, std::max(1u, std::thread::hardware_concurrency()));
+    std::atomic<size_t> next{0};
+    std::exception_ptr failure;
+    std::atomic<bool> failed{false};
+    auto worker = [&]() {
+      for (size_t i; !failed && (i = next++) < nat;) {
+        try {
+          fn(i);
+        } catch (...) {
+          if (!failed.exchange(true)) failure = std::current_exception();
+        }
+      }
+    };
+    std::vector<std::thread> pool;
+    for (size_t k = 1; k < nth; ++k) pool.emplace_back(worker);
+    worker();
+    for (auto& th : pool) th.join();
+    if (failure) std::rethrow_exception(failure);
+  };
+  parallel_atoms([&](size_t iat) {
     const Atom& at = (*mol)[iat];
     const double c[3] = {at.x, at.y, at.z};
     const AtomicGrid& g = mg->grids.at(at.Z);
@@ -79,31 +105,42 @@ std::shared_ptr<LoadBalancer> make_load_balancer(std::shared_ptr<const Molecule>
         }
         t.weights[i] = g.weights[b.first + i];
       }
-      t.shell_list = screen_box(*basis, lo, up, t.nbe);
-      if (t.shell_list.empty()) continue;
+      if (device) {
+        per_atom_box[iat].insert(per_atom_box[iat].end(), {lo[0], lo[1], lo[2], up[0], up[1], up[2]});
+      } else {
+        t.shell_list = screen_box(*basis, lo, up, t.nbe);
+        if (t.shell_list.empty()) continue;
+      }
       t.dist_nearest = lb->meta->dist_nearest[iat];
       per_atom[iat].push_back(std::move(t));
     }
-  };
-  {
-    const size_t nth = std::min<size_t>(nat, std::max(1u, std::thread::hardware_concurrency()));
-    std::atomic<size_t> next{0};
-    std::exception_ptr failure;
-    std::atomic<bool> failed{false};
-    auto worker = [&]() {
-      for (size_t i; !failed && (i = next++) < nat;) {
-        try {
-          atom_tasks(i);
-        } catch (...) {
-          if (!failed.exchange(true)) failure = std::current_exception();
-        }
+  });
+  if (device) {
+    // collision bitset of every candidate box on the device, decoded per atom
+    std::vector<size_t> first(nat + 1, 0);
+    for (size_t i = 0; i < nat; ++i) first[i + 1] = first[i] + per_atom[i].size();
+    std::vector<double> boxes;
+    boxes.reserve(6 * first[nat]);
+    for (const auto& v : per_atom_box) boxes.insert(boxes.end(), v.begin(), v.end());
+    std::vector<uint32_t> bits;
+    int nwords = 0;
+    screen_boxes_device(boxes, *basis, bits, nwords);
+    parallel_atoms([&](size_t iat) {
+      std::vector<XCTask> kept;
+      for (size_t k = 0; k < per_atom[iat].size(); ++k) {
+        XCTask& t = per_atom[iat][k];
+        const uint32_t* w = bits.data() + (first[iat] + k) * (size_t)nwords;
+        t.nbe = 0;
+        for (int q = 0; q < nwords; ++q)
+          for (uint32_t m = w[q]; m; m &= m - 1) {
+            const int sh = 32 * q + __builtin_ctz(m);
+            t.shell_list.push_back(sh);
+            t.nbe += basis->shells[sh].size();
+          }
+        if (!t.shell_list.empty()) kept.push_back(std::move(t));
       }
-    };
-    std::vector<std::thread> pool;
-    for (size_t k = 1; k < nth; ++k) pool.emplace_back(worker);
-    worker();
-    for (auto& th : pool) th.join();
-    if (failure) std::rethrow_exception(failure);
+      per_atom[iat].swap(kept);
+    });
   }
   std::vector<XCTask> tasks;
   for (auto& v : per_atom)

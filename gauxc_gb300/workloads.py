@@ -121,5 +121,7 @@ def build_system(sysd, device=True):
         mol, g.PruningScheme[sysd["pruning"]], sysd["batch_size"], g.RadialQuad.MuraKnowles,
         g.AtomicGridSizeDefault[sysd["grid"]])
     rt = g.DeviceRuntimeEnvironment(0.9) if device else g.RuntimeEnvironment()
-    lb = g.LoadBalancerFactory(g.ExecutionSpace.Device, "Default").get_instance(rt, mol, mg, basis)
+    # the Device load balancer screens on the GPU; the Host one on the host
+    ex = g.ExecutionSpace.Device if device else g.ExecutionSpace.Host
+    lb = g.LoadBalancerFactory(ex, "Default").get_instance(rt, mol, mg, basis)
     return mol, basis, mg, lb

@@ -18,7 +18,8 @@ def benzene_system(g, fname, tol=EPS, prune="Unpruned", grid="UltraFineGrid", de
                                                  g.RadialQuad.MuraKnowles,
                                                  g.AtomicGridSizeDefault[grid])
     rt = g.DeviceRuntimeEnvironment(0.9) if device else g.RuntimeEnvironment()
-    lb = g.LoadBalancerFactory(g.ExecutionSpace.Device, "Default").get_instance(rt, mol, mg, basis)
+    ex = g.ExecutionSpace.Device if device else g.ExecutionSpace.Host
+    lb = g.LoadBalancerFactory(ex, "Default").get_instance(rt, mol, mg, basis)
     return d, mol, basis, mg, lb
 
 

@@ -59,15 +59,16 @@ def test_factory_errors(g):
         g.DeviceRuntimeEnvironment(1.5)
 
 
-def _tiny_system(g):
+def _tiny_system(g, ex=None):
     mol = g.Molecule([(1, 0.0, 0.0, 0.0), (1, 0.0, 0.0, 1.4)])
     basis = g.BasisSet([g.Shell(0, [1.0], [1.0], (0.0, 0.0, 0.0)),
                         g.Shell(0, [1.0], [1.0], (0.0, 0.0, 1.4))])
     mg = g.MolGridFactory.create_default_molgrid(mol, g.PruningScheme.Unpruned, 128,
                                                  g.RadialQuad.MuraKnowles,
                                                  g.AtomicGridSizeDefault.FineGrid)
-    lb = g.LoadBalancerFactory(g.ExecutionSpace.Device, "Default").get_instance(
-        g.DeviceRuntimeEnvironment(0.5), mol, mg, basis)
+    lb = g.LoadBalancerFactory(ex if ex is not None else g.ExecutionSpace.Host,
+                               "Default").get_instance(g.DeviceRuntimeEnvironment(0.5), mol, mg,
+                                                       basis)
     return mol, basis, lb
 
 
@@ -96,6 +97,8 @@ def test_device_paths_fail_loudly_without_gpu(g):
     mw = g.MolecularWeightsFactory(g.ExecutionSpace.Device).get_instance()
     with pytest.raises(GauXCError, match="no CUDA device"):
         mw.modify_weights(lb)
+    with pytest.raises(GauXCError, match="no CUDA device"):
+        _tiny_system(g, g.ExecutionSpace.Device)  # the Device load balancer screens on the GPU
     with pytest.raises(GauXCError, match="no CUDA device"):
         g.collocation(basis, np.zeros((4, 3)), [0, 1])
 
