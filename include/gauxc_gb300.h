@@ -6,7 +6,7 @@
  * argument order and error behaviour (every call takes a GauXCStatus*; on
  * failure status->code is non-zero and status->message holds a malloc'd
  * string that gauxc_status_delete frees).  A code written against the
- * reference headers (include/gauxc/c/*.h) links against this library for the
+ * reference headers (include/gauxc/c/ *.h) links against this library for the
  * functions below.  Each declaration cites the reference declaration it
  * replaces.
  *

@@ -182,3 +182,46 @@ def eval_exc_vxc(basis, tasks, P, func, want_vxc=True, nthreads=0):
                               V.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) if V is not None else None,
                               _p(en), ctypes.c_int(nthreads))
     return en[0], V, en[1]
+
+
+def functional_pol(name, rho, sigma=None):
+    """Polarized functional: rho[n, 2] (alpha, beta), sigma[n, 3] (aa, ab, bb).
+    Returns eps[n], vrho[n, 2], vsigma[n, 3]."""
+    kind, xs, cs, kappa, mu, _ = FUNCTIONALS[name.upper()]
+    rho = np.ascontiguousarray(rho, dtype=np.float64).reshape(-1, 2)
+    n = len(rho)
+    sg = None if sigma is None else np.ascontiguousarray(sigma, dtype=np.float64).reshape(-1, 3)
+    eps, vr, vs = np.zeros(n), np.zeros((n, 2)), np.zeros((n, 3))
+    lib().oracle_functional_pol(ctypes.c_int(kind), ctypes.c_double(xs), ctypes.c_double(cs),
+                                ctypes.c_double(kappa), ctypes.c_double(mu), ctypes.c_int64(n),
+                                _p(rho), _p(sg), _p(eps), _p(vr), _p(vs))
+    return eps, vr, vs
+
+
+def eval_exc_vxc_uks(basis, tasks, Ps, Pz, func, want_vxc=True, nthreads=0):
+    """UKS: Ps = Pa + Pb, Pz = Pa - Pb.  Returns (EXC, VXCs, VXCz, N_el)."""
+    kind, xs, cs, kappa, mu, gga = FUNCTIONALS[func.upper()]
+    pt_off = np.zeros(len(tasks) + 1, np.int64)
+    sh_off = np.zeros(len(tasks) + 1, np.int64)
+    for i, (p, w, s) in enumerate(tasks):
+        pt_off[i + 1] = pt_off[i] + len(w)
+        sh_off[i + 1] = sh_off[i] + len(s)
+    pts = np.ascontiguousarray(np.concatenate([np.asarray(t[0]).reshape(-1, 3) for t in tasks]))
+    wts = np.ascontiguousarray(np.concatenate([t[1] for t in tasks]))
+    sl = np.ascontiguousarray(np.concatenate([t[2] for t in tasks]).astype(np.int32))
+    nbf = basis.nbf
+    A = np.asfortranarray(Ps, dtype=np.float64)
+    Bz = np.asfortranarray(Pz, dtype=np.float64)
+    Vs = np.zeros((nbf, nbf), order="F") if want_vxc else None
+    Vz = np.zeros((nbf, nbf), order="F") if want_vxc else None
+    en = np.zeros(2)
+    dp = ctypes.POINTER(ctypes.c_double)
+    lib().oracle_eval_exc_vxc_uks(*basis.args(), ctypes.c_int(nbf), ctypes.c_int(len(tasks)),
+                                  _i64(pt_off), _p(pts), _p(wts), _i64(sh_off), _i32(sl),
+                                  ctypes.c_int(kind), ctypes.c_double(xs), ctypes.c_double(cs),
+                                  ctypes.c_double(kappa), ctypes.c_double(mu), ctypes.c_int(gga),
+                                  A.ctypes.data_as(dp), Bz.ctypes.data_as(dp),
+                                  Vs.ctypes.data_as(dp) if Vs is not None else None,
+                                  Vz.ctypes.data_as(dp) if Vz is not None else None,
+                                  _p(en), ctypes.c_int(nthreads))
+    return en[0], Vs, Vz, en[1]

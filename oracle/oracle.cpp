@@ -135,6 +135,187 @@ void eval_functional(const Func& f, double rho, double sigma, double& eps, doubl
   vs = e.s;
 }
 
+// ------------------------------------------------------------------ polarized
+// Spin-polarized functionals (UKS): inputs rho_a, rho_b, sigma_aa, sigma_ab,
+// sigma_bb; forward-mode duals carry the five first derivatives.
+//   Slater     e_x = (e_x[2 rho_a] + e_x[2 rho_b]) / 2 (spin scaling)
+//   VWN        paramagnetic and ferromagnetic RPA fits of Vosko, Wilk and
+//              Nusair (1980) joined by the exchange-like interpolation
+//              e = e_P + f(z) (e_F - e_P); this is the form that reproduces
+//              the reference's UKS SVWN5 golden (cytosine, dEXC 1.3e-9 Eh,
+//              |dVXC_s|/nbf 7e-12), where the spin-stiffness form misses EXC
+//              by 6e-4 Eh
+//   PBE x      spin scaling of the unpolarized PBE exchange (kappa, mu)
+//   PBE c      PW92 e_c(rs, z) (the three PW92 fits, modified A values as
+//              in the unpolarized oracle) + H(rs, z, t) with
+//              phi = ((1 + z)^(2/3) + (1 - z)^(2/3)) / 2
+// Density cutoffs: no contribution for rho_a + rho_b <= 1e-15 (PBE c:
+// 1e-12), a spin channel's exchange vanishes at rho_s <= 1e-15 / 2, and
+// |z| is kept at or below 1 - 1e-12.
+constexpr int NP = 5;
+struct DP {
+  double v;
+  double d[NP];
+};
+inline DP cst(double v) {
+  DP r{v, {0, 0, 0, 0, 0}};
+  return r;
+}
+inline DP var(double v, int i) {
+  DP r = cst(v);
+  r.d[i] = 1.;
+  return r;
+}
+inline DP operator+(DP a, DP b) {
+  for (int i = 0; i < NP; ++i) a.d[i] += b.d[i];
+  a.v += b.v;
+  return a;
+}
+inline DP operator-(DP a, DP b) {
+  for (int i = 0; i < NP; ++i) a.d[i] -= b.d[i];
+  a.v -= b.v;
+  return a;
+}
+inline DP operator*(DP a, DP b) {
+  DP r{a.v * b.v, {}};
+  for (int i = 0; i < NP; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
+  return r;
+}
+inline DP operator/(DP a, DP b) {
+  const double q = 1. / b.v;
+  DP r{a.v * q, {}};
+  for (int i = 0; i < NP; ++i) r.d[i] = (a.d[i] * b.v - a.v * b.d[i]) * q * q;
+  return r;
+}
+inline DP operator*(double c, DP a) {
+  a.v *= c;
+  for (int i = 0; i < NP; ++i) a.d[i] *= c;
+  return a;
+}
+inline DP operator*(DP a, double c) { return c * a; }
+inline DP operator+(DP a, double c) { a.v += c; return a; }
+inline DP operator+(double c, DP a) { a.v += c; return a; }
+inline DP operator-(DP a, double c) { a.v -= c; return a; }
+inline DP operator-(double c, DP a) { return cst(c) - a; }
+inline DP operator/(DP a, double c) { return (1. / c) * a; }
+inline DP operator/(double c, DP a) { return cst(c) / a; }
+inline DP pchain(DP a, double f, double df) {
+  DP r{f, {}};
+  for (int i = 0; i < NP; ++i) r.d[i] = df * a.d[i];
+  return r;
+}
+inline DP plog(DP a) { return pchain(a, std::log(a.v), 1. / a.v); }
+inline DP pexp(DP a) { const double e = std::exp(a.v); return pchain(a, e, e); }
+inline DP psqrt(DP a) { const double q = std::sqrt(a.v); return pchain(a, q, 0.5 / q); }
+inline DP patan(DP a) { return pchain(a, std::atan(a.v), 1. / (1. + a.v * a.v)); }
+inline DP ppow(DP a, double p) { return pchain(a, std::pow(a.v, p), p * std::pow(a.v, p - 1.)); }
+
+// one VWN fit: A, b, c, x0 at x = sqrt(rs)
+DP vwn_fit(DP x, double A, double b, double c, double x0) {
+  const double Q = std::sqrt(4 * c - b * b);
+  const double X0 = x0 * x0 + b * x0 + c;
+  DP X = x * x + b * x + c;
+  DP at = patan(Q / (2. * x + b));
+  return A * (plog(x * x / X) + (2. * b / Q) * at -
+              (b * x0 / X0) * (plog((x - x0) * (x - x0) / X) + (2. * (b + 2. * x0) / Q) * at));
+}
+
+// one PW92 fit G(rs) (p = 1)
+DP pw92_fit(DP rs, double A, double a1, double b1, double b2, double b3, double b4) {
+  DP s = psqrt(rs);
+  DP den = 2. * A * (b1 * s + b2 * rs + b3 * rs * s + b4 * rs * rs);
+  return -2. * A * (1. + a1 * rs) * plog(1. + 1. / den);
+}
+
+const double FZ20 = 1.709920934161365617563962776245;  // f''(0)
+
+DP fzeta(DP z) {
+  return (ppow(1. + z, 4. / 3.) + ppow(1. - z, 4. / 3.) - 2.) / (std::pow(2., 4. / 3.) - 2.);
+}
+
+DP slater_pol(DP ra, DP rb) {
+  const double cx = -0.75 * std::pow(3. / PI, 1. / 3.);
+  DP e = cst(0.);
+  if (ra.v > 0.5e-15) e = e + 0.5 * cx * ppow(2. * ra, 4. / 3.);
+  if (rb.v > 0.5e-15) e = e + 0.5 * cx * ppow(2. * rb, 4. / 3.);
+  return e;
+}
+
+DP zeta_of(DP ra, DP rb) {
+  DP z = (ra - rb) / (ra + rb);
+  const double lim = 1. - 1e-12;
+  if (z.v > lim) z = cst(lim);
+  if (z.v < -lim) z = cst(-lim);
+  return z;
+}
+
+DP vwn_pol(DP ra, DP rb) {
+  DP rho = ra + rb;
+  DP rs = ppow(3. / (4. * PI * rho), 1. / 3.);
+  DP x = psqrt(rs);
+  DP z = zeta_of(ra, rb);
+  DP eP = vwn_fit(x, 0.0310907, 13.0720, 42.7198, -0.409286);
+  DP eF = vwn_fit(x, 0.01554535, 20.1231, 101.578, -0.743294);
+  return rho * (eP + fzeta(z) * (eF - eP));
+}
+
+DP pbe_x_pol(DP ra, DP rb, DP saa, DP sbb, double kappa, double mu) {
+  auto one = [&](DP r2, DP s4) {  // unpolarized PBE exchange at (2 rho_s, 4 sigma_ss)
+    DP kf = ppow(3. * PI * PI * r2, 1. / 3.);
+    DP s2 = s4 / (4. * kf * kf * r2 * r2);
+    DP F = 1. + kappa - kappa / (1. + mu * s2 / kappa);
+    return -0.75 * std::pow(3. / PI, 1. / 3.) * ppow(r2, 4. / 3.) * F;
+  };
+  DP e = cst(0.);
+  if (ra.v > 0.5e-15) e = e + 0.5 * one(2. * ra, 4. * saa);
+  if (rb.v > 0.5e-15) e = e + 0.5 * one(2. * rb, 4. * sbb);
+  return e;
+}
+
+DP pbe_c_pol(DP ra, DP rb, DP saa, DP sab, DP sbb) {
+  const double beta = 0.06672455060314922;
+  const double gamma = (1. - std::log(2.)) / (PI * PI);
+  DP rho = ra + rb;
+  DP rs = ppow(3. / (4. * PI * rho), 1. / 3.);
+  DP z = zeta_of(ra, rb);
+  DP e0 = pw92_fit(rs, 0.0310907, 0.21370, 7.5957, 3.5876, 1.6382, 0.49294);
+  DP e1 = pw92_fit(rs, 0.01554535, 0.20548, 14.1189, 6.1977, 3.3662, 0.62517);
+  DP mac = pw92_fit(rs, 0.0168869, 0.11125, 10.357, 3.6231, 0.88026, 0.49671);  // -alpha_c
+  DP f = fzeta(z);
+  DP z4 = z * z * z * z;
+  DP ec = e0 - mac * f * (1. - z4) / FZ20 + (e1 - e0) * f * z4;
+  DP phi = 0.5 * (ppow(1. + z, 2. / 3.) + ppow(1. - z, 2. / 3.));
+  DP phi3 = phi * phi * phi;
+  DP kf = ppow(3. * PI * PI * rho, 1. / 3.);
+  DP ks = psqrt(4. * kf / PI);
+  DP sig = saa + 2. * sab + sbb;
+  DP t2 = sig / (4. * phi * phi * ks * ks * rho * rho);
+  DP A = (beta / gamma) / (pexp(-1. * ec / (gamma * phi3)) - 1.);
+  DP At2 = A * t2;
+  DP H = gamma * phi3 * plog(1. + (beta / gamma) * t2 * (1. + At2) / (1. + At2 + At2 * At2));
+  return rho * (ec + H);
+}
+
+// eps (per particle), vrho[2], vsigma[3] of a polarized functional.
+void eval_functional_pol(const Func& f, double rhoa, double rhob, double saa, double sab,
+                         double sbb, double& eps, double* vr, double* vs) {
+  DP ra = var(rhoa, 0), rb = var(rhob, 1), Sa = var(saa, 2), Sab = var(sab, 3), Sb = var(sbb, 4);
+  const double rho = rhoa + rhob;
+  DP e = cst(0.);
+  if (f.kind == 0) {
+    if (rho > 1e-15) e = e + f.xs * slater_pol(ra, rb) + f.cs * vwn_pol(ra, rb);
+  } else {
+    if (rho > 1e-15) e = e + f.xs * pbe_x_pol(ra, rb, Sa, Sb, f.kappa, f.mu);
+    if (rho > 1e-12) e = e + f.cs * pbe_c_pol(ra, rb, Sa, Sab, Sb);
+  }
+  eps = rho > 0. && e.v != 0. ? e.v / rho : 0.;
+  vr[0] = e.d[0];
+  vr[1] = e.d[1];
+  vs[0] = e.d[2];
+  vs[1] = e.d[3];
+  vs[2] = e.d[4];
+}
+
 // ------------------------------------------------------------------ shells
 struct Mono {
   double c;
@@ -554,6 +735,175 @@ void oracle_eval_exc_vxc(int nshells_basis, const int32_t* l, const int32_t* pur
       for (int i = j + 1; i < nbf; ++i) VXC[(size_t)i * nbf + j] = VXC[(size_t)j * nbf + i];
   exc_nel[0] = EXC;
   exc_nel[1] = NEL;
+}
+
+// UKS: Ps = P_a + P_b, Pz = P_a - P_b (nbf x nbf column-major); VXCs / VXCz
+// (may be null) and exc_nel[2].  reference_replicated_xc_host_integrator_exc_vxc.hpp:
+// X factor 1 for both densities (:387-394); rho_+- = (rho_s +- rho_z) / 2,
+// grad n = 2 grad(phi) X_s, grad M = 2 grad(phi) X_z and the three sigmas of
+// eval_uvvar_gga_uks (reference_local_host_work_driver.cxx:270-327); Z_s and
+// Z_z of eval_zmat_{lda,gga}_vxc_uks (:607-631, :715-770).
+void oracle_eval_exc_vxc_uks(int nshells_basis, const int32_t* l, const int32_t* pure,
+                             const int32_t* nprim, const double* alpha, const double* coeff,
+                             const double* origin, int nbf, int ntasks, const int64_t* pt_off,
+                             const double* pts, const double* wts, const int64_t* sh_off,
+                             const int32_t* shell_list, int kind, double xs, double cs,
+                             double kappa, double mu, int gga, const double* Ps, const double* Pz,
+                             double* VXCs, double* VXCz, double* exc_nel, int nthreads) {
+  Basis B(nshells_basis, l, pure, nprim, alpha, coeff, origin);
+  const Func func{kind, xs, cs, kappa, mu};
+  const bool vxc = VXCs && VXCz;
+  if (vxc) {
+    std::memset(VXCs, 0, sizeof(double) * (size_t)nbf * nbf);
+    std::memset(VXCz, 0, sizeof(double) * (size_t)nbf * nbf);
+  }
+  double EXC = 0., NEL = 0.;
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel reduction(+ : EXC, NEL)
+  {
+    std::vector<double> f, fx, fy, fz, Pss, Pzs, Xs, Xz, Zs, Zz, V;
+#pragma omp for schedule(dynamic, 1)
+    for (int t = 0; t < ntasks; ++t) {
+      const int npts = (int)(pt_off[t + 1] - pt_off[t]);
+      const int nsh = (int)(sh_off[t + 1] - sh_off[t]);
+      const int32_t* sl = shell_list + sh_off[t];
+      const double* tp = pts + 3 * pt_off[t];
+      const double* tw = wts + pt_off[t];
+      std::vector<int> bf;
+      for (int i = 0; i < nsh; ++i)
+        for (int k = 0; k < B.size(sl[i]); ++k) bf.push_back(B.ao_off[sl[i]] + k);
+      const int nbe = (int)bf.size();
+      const size_t ne = (size_t)npts * nbe;
+      f.assign(ne, 0.);
+      if (gga) {
+        fx.assign(ne, 0.);
+        fy.assign(ne, 0.);
+        fz.assign(ne, 0.);
+      }
+      collocate(B, npts, tp, nsh, sl, nbe, f.data(), gga ? fx.data() : nullptr,
+                gga ? fy.data() : nullptr, gga ? fz.data() : nullptr);
+      Pss.resize((size_t)nbe * nbe);
+      Pzs.resize((size_t)nbe * nbe);
+      for (int j = 0; j < nbe; ++j)
+        for (int i = 0; i < nbe; ++i) {
+          Pss[(size_t)j * nbe + i] = Ps[(size_t)bf[j] * nbf + bf[i]];
+          Pzs[(size_t)j * nbe + i] = Pz[(size_t)bf[j] * nbf + bf[i]];
+        }
+      Xs.resize(ne);
+      Xz.resize(ne);
+      if (g_dgemm) {
+        const double one = 1.0, zero = 0.0;
+        g_dgemm("N", "N", &nbe, &npts, &nbe, &one, Pss.data(), &nbe, f.data(), &nbe, &zero,
+                Xs.data(), &nbe);
+        g_dgemm("N", "N", &nbe, &npts, &nbe, &one, Pzs.data(), &nbe, f.data(), &nbe, &zero,
+                Xz.data(), &nbe);
+      } else {
+        gemm(nbe, npts, nbe, 1.0, Pss.data(), nbe, f.data(), nbe, false, Xs.data(), nbe);
+        gemm(nbe, npts, nbe, 1.0, Pzs.data(), nbe, f.data(), nbe, false, Xz.data(), nbe);
+      }
+      std::vector<double> as(npts), az(npts), bs(3 * (size_t)npts), bz(3 * (size_t)npts);
+      double exc_t = 0., nel_t = 0.;
+      for (int p = 0; p < npts; ++p) {
+        const size_t o = (size_t)p * nbe;
+        double rs_ = 0., rz = 0., gn[3] = {0, 0, 0}, gm[3] = {0, 0, 0};
+        for (int i = 0; i < nbe; ++i) {
+          rs_ += f[o + i] * Xs[o + i];
+          rz += f[o + i] * Xz[o + i];
+        }
+        if (gga) {
+          const double* d[3] = {fx.data() + o, fy.data() + o, fz.data() + o};
+          for (int a = 0; a < 3; ++a) {
+            for (int i = 0; i < nbe; ++i) {
+              gn[a] += d[a][i] * Xs[o + i];
+              gm[a] += d[a][i] * Xz[o + i];
+            }
+            gn[a] *= 2.;
+            gm[a] *= 2.;
+          }
+        }
+        const double ra = 0.5 * (rs_ + rz), rb = 0.5 * (rs_ - rz);
+        const double nn = gn[0] * gn[0] + gn[1] * gn[1] + gn[2] * gn[2];
+        const double mm = gm[0] * gm[0] + gm[1] * gm[1] + gm[2] * gm[2];
+        const double nm = gn[0] * gm[0] + gn[1] * gm[1] + gn[2] * gm[2];
+        const double saa = 0.25 * (nn + mm) + 0.5 * nm, sab = 0.25 * (nn - mm),
+                     sbb = 0.25 * (nn + mm) - 0.5 * nm;
+        double eps, vr[2], vs[3];
+        eval_functional_pol(func, ra, rb, saa, sab, sbb, eps, vr, vs);
+        const double w = tw[p];
+        exc_t += (eps * w) * (ra + rb);
+        nel_t += w * (ra + rb);
+        const double fp = 0.5 * w * vr[0], fm = 0.5 * w * vr[1];
+        as[p] = 0.5 * (fp + fm);
+        az[p] = 0.5 * (fp - fm);
+        const double g1 = 0.5 * w * (vs[0] + vs[1] + vs[2]), g2 = 0.5 * w * (vs[0] - vs[2]),
+                     g3 = 0.5 * w * (vs[0] - vs[1] + vs[2]);
+        for (int a = 0; a < 3; ++a) {
+          bs[3 * p + a] = gga ? g1 * gn[a] + g2 * gm[a] : 0.;
+          bz[3 * p + a] = gga ? g3 * gm[a] + g2 * gn[a] : 0.;
+        }
+      }
+      EXC += exc_t;
+      NEL += nel_t;
+      if (!vxc) continue;
+      Zs.resize(ne);
+      Zz.resize(ne);
+      for (int p = 0; p < npts; ++p)
+        for (int i = 0; i < nbe; ++i) {
+          const size_t o = (size_t)p * nbe + i;
+          double zs = as[p] * f[o], zz = az[p] * f[o];
+          if (gga) {
+            zs += bs[3 * p] * fx[o] + bs[3 * p + 1] * fy[o] + bs[3 * p + 2] * fz[o];
+            zz += bz[3 * p] * fx[o] + bz[3 * p + 1] * fy[o] + bz[3 * p + 2] * fz[o];
+          }
+          Zs[o] = zs;
+          Zz[o] = zz;
+        }
+      V.resize((size_t)nbe * nbe);
+      for (int which = 0; which < 2; ++which) {
+        const double* Z = which ? Zz.data() : Zs.data();
+        double* OUT = which ? VXCz : VXCs;
+        if (g_dsyr2k) {
+          const double one = 1.0, zero = 0.0;
+          g_dsyr2k("L", "N", &nbe, &npts, &one, f.data(), &nbe, Z, &nbe, &zero, V.data(), &nbe);
+        } else {
+          gemm(nbe, nbe, npts, 1.0, f.data(), nbe, Z, nbe, true, V.data(), nbe);
+        }
+        for (int j = 0; j < nbe; ++j)
+          for (int i = j; i < nbe; ++i) {
+            const double v = g_dsyr2k ? V[(size_t)j * nbe + i]
+                                      : V[(size_t)j * nbe + i] + V[(size_t)i * nbe + j];
+            const int gi = bf[i], gj = bf[j];
+            const int r_ = std::max(gi, gj), c_ = std::min(gi, gj);
+#pragma omp atomic
+            OUT[(size_t)c_ * nbf + r_] += v;
+          }
+      }
+    }
+  }
+  if (vxc)
+    for (int j = 0; j < nbf; ++j)
+      for (int i = j + 1; i < nbf; ++i) {
+        VXCs[(size_t)i * nbf + j] = VXCs[(size_t)j * nbf + i];
+        VXCz[(size_t)i * nbf + j] = VXCz[(size_t)j * nbf + i];
+      }
+  exc_nel[0] = EXC;
+  exc_nel[1] = NEL;
+}
+
+// Polarized functional on npts points: rho[2 i + s], sigma[3 i + k] (may be
+// null for LDA); eps[i], vrho[2 i + s], vsigma[3 i + k].
+void oracle_functional_pol(int kind, double xs, double cs, double kappa, double mu, int64_t npts,
+                           const double* rho, const double* sigma, double* eps, double* vrho,
+                           double* vsigma) {
+  const Func f{kind, xs, cs, kappa, mu};
+  for (int64_t i = 0; i < npts; ++i) {
+    double vs[3];
+    eval_functional_pol(f, rho[2 * i], rho[2 * i + 1], sigma ? sigma[3 * i] : 0.,
+                        sigma ? sigma[3 * i + 1] : 0., sigma ? sigma[3 * i + 2] : 0., eps[i],
+                        vrho + 2 * i, vs);
+    if (vsigma)
+      for (int k = 0; k < 3; ++k) vsigma[3 * i + k] = vs[k];
+  }
 }
 
 }  // extern "C"

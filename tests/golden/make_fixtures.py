@@ -14,6 +14,9 @@ Sources (reference paths):
   tests/ref_data/benzene_pbe0_cc-pvdz_ufg_ssf.hdf5             -> benzene_pbe0.npz
       (molecule, normalized basis, alpha density P, VXC, EXC; read as in
        tests/xc_integrator.cxx:47-106)
+  tests/ref_data/cytosine_svwn5_cc-pvdz_ufg_ssf_robust_uks.hdf5 -> cytosine_svwn5_uks.npz
+      (UKS: scalar and z densities, VXC_SCALAR / VXC_Z, EXC;
+       tests/xc_integrator.cxx:218-236)
   tests/ref_data/benzene_weights_ssf.hdf5                      -> benzene_weights_ssf.npz
       (points, unmodified and SSF-modified weights per task; every
        ``POINT_STRIDE``-th point is kept: SSF acts point by point)
@@ -71,6 +74,20 @@ def xc_case(fname, out):
     # symmetric so the orientation does not matter.
     d["P"] = f.read("/DENSITY")
     d["VXC"] = f.read("/VXC")
+    d["EXC"] = np.array(f.read("/EXC")).reshape(-1)[:1]
+    np.savez_compressed(os.path.join(HERE, out), **d)
+
+
+def uks_case(fname, out):
+    """UKS golden: scalar / z densities (Ps = Pa + Pb, Pz = Pa - Pb) and the
+    two VXC matrices (tests/xc_integrator.cxx:218-236)."""
+    f = H5File(os.path.join(DATA, fname))
+    Z, xyz = mol_arrays(f)
+    d = dict(Z=Z, xyz=xyz, **basis_arrays(f))
+    d["Ps"] = f.read("/DENSITY_SCALAR")
+    d["Pz"] = f.read("/DENSITY_Z")
+    d["VXCs"] = f.read("/VXC_SCALAR")
+    d["VXCz"] = f.read("/VXC_Z")
     d["EXC"] = np.array(f.read("/EXC")).reshape(-1)[:1]
     np.savez_compressed(os.path.join(HERE, out), **d)
 
@@ -198,6 +215,7 @@ if __name__ == "__main__":
     xc_case("benzene_svwn5_cc-pvdz_ufg_ssf.hdf5", "benzene_svwn5.npz")
     xc_case("benzene_svwn5_cc-pvdz_ufg_ssf_treutler_prune.hdf5", "benzene_svwn5_treutler.npz")
     xc_case("benzene_pbe0_cc-pvdz_ufg_ssf.hdf5", "benzene_pbe0.npz")
+    uks_case("cytosine_svwn5_cc-pvdz_ufg_ssf_robust_uks.hdf5", "cytosine_svwn5_uks.npz")
     weights_case()
     collocation_case()
     tasks_case()

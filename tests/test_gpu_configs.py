@@ -45,17 +45,18 @@ def _system(g, idx, ntasks):
         g.MolecularWeightsFactory(g.ExecutionSpace.Device).get_instance().modify_weights(sub)
         tasks = sub.get_tasks()
         # device SSF weights of the sample against the oracle's host algorithm
-        # (weights.cxx).  Cell products truncated at 1e-13 in different
-        # orders differ at that level: on 256 waters the reference's device
-        # kernel (atom-index order) lands up to 6e-10 of the weight away from
-        # the host algorithm and this build's screened kernel (nearest atoms
-        # first) up to 3e-11 (CPU emulation of both); the reference's own
-        # check is Catch's default Approx, 1.2e-5 relative
+        # (weights.cxx).  Cell products are truncated at 1e-13, and where the
+        # sum of a point's cell products is small the truncation order shows:
+        # on 23,060 points of 256 waters (CPU emulation of both kernels) the
+        # reference's device kernel (atom-index order, cuda_ssf_1d.cu) lands
+        # up to 3.5e-9 of the weight away from the host algorithm and this
+        # build's screened kernel (nearest atoms first) up to 6.2e-9; the
+        # reference's own check is Catch's default Approx, 1.2e-5 relative
         # (tests/weights_cuda.hpp:115).
         pts, w0, ip, dn = flat_points(tasks0)
         wo = oracle.ssf_weights(pts, ip, dn, mol.coords(), w0)
         wd = np.concatenate([t["weights"] for t in tasks])
-        assert np.all(np.abs(wd - wo) <= 2e-10 * np.abs(w0))
+        assert np.all(np.abs(wd - wo) <= 1e-8 * np.abs(w0))
         ref = oracle.eval_exc_vxc(oracle_basis(basis),
                                   [(t["points"], t["weights"], t["shell_list"]) for t in tasks],
                                   s["P"], s["functional"])

@@ -94,9 +94,12 @@ def _noalloc_weights(g, pts, ip, dn, coords, w0):
 
 def test_screened_ssf_on_256_waters(g):
     """Screened kernel vs the host algorithm and the reference-order kernel on
-    a strided sample of workload 4's points (768 atoms).  Measured on the CPU
-    (emulation of both kernels): the reference order lands up to 6e-10 of the
-    weight away from the host algorithm, the screened order up to 3e-11."""
+    a strided sample of workload 4's points (768 atoms, every 400th task:
+    23,060 points).  Cell products truncated at 1e-13 in different orders
+    differ where a point's cell products sum to little; measured on the CPU
+    (emulation of both kernels on these points): reference order vs host
+    algorithm up to 3.5e-9 of the weight, screened vs host 6.2e-9, screened vs
+    reference order 2.7e-9."""
     from gauxc_gb300 import workloads as W
     s = W.config(4)["systems"][0]
     mol, basis, mg, lb = W.build_system(s, device=False)
@@ -108,9 +111,11 @@ def test_screened_ssf_on_256_waters(g):
     t_s = time.perf_counter() - t0
     wo = oracle.ssf_weights(pts, ip, dn, co, w0)
     wr = _noalloc_weights(g, pts, ip, dn, co, w0)
-    assert np.all(np.abs(ws - wo) <= 2e-10 * np.abs(w0))
+    assert np.all(np.abs(ws - wo) <= 1e-8 * np.abs(w0))
     assert np.all(np.abs(wr - wo) <= 1e-8 * np.abs(w0))
     assert np.all(np.abs(ws - wr) <= 1e-8 * np.abs(w0))
+    # the bulk agrees far more closely than the worst points
+    assert np.median(np.abs(ws - wo) / np.abs(w0)) <= 1e-14
     print(f"\n{len(w0)} points: screened SSF {t_s:.3f} s (with transfers); max rel. diff "
           f"screened/host {np.max(np.abs(ws - wo) / np.abs(w0)):.2e}, reference-order/host "
           f"{np.max(np.abs(wr - wo) / np.abs(w0)):.2e}")

@@ -97,3 +97,55 @@ def test_functional_derivatives_finite_difference():
             em, _, _ = oracle.functional(name, rho, sig - hs)
             ds = rho * (ep - em) / (2 * hs)
             np.testing.assert_allclose(vs, ds, rtol=1e-4, atol=1e-14)
+
+
+def test_uks_svwn5_matches_golden():
+    """UKS (cytosine doublet, SVWN5, cc-pVDZ, UltraFine, Robust pruning, tol = eps;
+    tests/xc_integrator.cxx:455-458): oracle with its own SSF weights.  The
+    reference's tolerance: EXC rel 1.2e-5, ||dVXC||_F / nbf < 1e-10."""
+    import gauxc_gb300 as g
+    from helpers import oracle_basis, oracle_ssf_tasks
+    d, mol, basis, mg, lb = benzene_system(g, "cytosine_svwn5_uks.npz", prune="Robust",
+                                           device=False)
+    tasks = oracle_ssf_tasks(lb.get_tasks(), mol.coords())
+    e, Vs, Vz, n = oracle.eval_exc_vxc_uks(oracle_basis(basis), tasks, d["Ps"], d["Pz"], "SVWN5")
+    nbf = len(Vs)
+    assert abs(e - d["EXC"][0]) <= 5e-9
+    assert np.linalg.norm(Vs - d["VXCs"]) / nbf <= 2e-11
+    assert np.linalg.norm(Vz - d["VXCz"]) / nbf <= 1e-12
+    assert abs(n - 57.0) < 1e-4  # cytosine C4H5N3O: 58 electrons minus one (doublet cation)
+
+
+@pytest.mark.parametrize("func", ["SVWN5", "PBE", "PBE0", "REVPBE"])
+def test_polarized_functional_unpolarized_limit(func):
+    """rho_a = rho_b = rho / 2, sigma_ss = sigma / 4: the polarized functional
+    equals the unpolarized one (energy, d/drho, d/dsigma)."""
+    rng = np.random.default_rng(11)
+    rho = 10.0 ** rng.uniform(-8, 2, 400)
+    sigma = rho ** (8 / 3) * 10.0 ** rng.uniform(-3, 2, 400)
+    e0, vr0, vs0 = oracle.functional(func, rho, sigma)
+    e1, vr1, vs1 = oracle.functional_pol(func, np.stack([rho / 2, rho / 2], 1),
+                                         np.stack([sigma / 4] * 3, 1))
+    assert np.allclose(e1, e0, rtol=1e-10, atol=1e-300)
+    assert np.allclose(vr1[:, 0], vr0, rtol=1e-9, atol=1e-300)
+    assert np.allclose(vr1[:, 1], vr0, rtol=1e-9, atol=1e-300)
+    if func != "SVWN5":
+        # the three partials cancel in their sum: compare on their own scale
+        assert np.all(np.abs(vs1.sum(1) / 4 - vs0) <= 1e-13 * np.abs(vs1).sum(1))
+
+
+def test_uks_closed_shell_equals_rks():
+    """Ps = 2 P, Pz = 0: UKS gives the RKS EXC and VXC_s = VXC, VXC_z = 0."""
+    import gauxc_gb300 as g
+    from gauxc_gb300 import workloads as W
+    from helpers import oracle_basis, oracle_ssf_tasks
+    s = W.config(5)["systems"][0]
+    mol, basis, mg, lb = W.build_system(s, device=False)
+    tasks = oracle_ssf_tasks(lb.get_tasks(), mol.coords())[::7]
+    ob = oracle_basis(basis)
+    e, V, n = oracle.eval_exc_vxc(ob, tasks, s["P"], "PBE")
+    eu, Vs, Vz, nu = oracle.eval_exc_vxc_uks(ob, tasks, 2 * s["P"], np.zeros_like(s["P"]), "PBE")
+    assert abs(eu - e) <= 1e-10 * abs(e)
+    assert np.abs(Vs - V).max() <= 1e-10 * np.abs(V).max()
+    assert np.abs(Vz).max() == 0.0
+    assert abs(nu - n) <= 1e-12 * n
