@@ -371,7 +371,7 @@ class MolecularWeightsFactory(_Handle):
 
 # ------------------------------------------------------------------ functional / integrator
 class functional_type(_Handle):
-    """XC functional by name: SVWN5, PBE, revPBE, PBE0 (unpolarized)."""
+    """XC functional by name: SVWN5, PBE, revPBE, PBE0; polarized=True for UKS."""
     _delete = "gauxc_functional_delete"
 
     def __init__(self, name, polarized=False):
@@ -397,6 +397,32 @@ class XCIntegrator(_Handle):
               ctypes.c_int64(P.shape[0]), ctypes.byref(exc),
               VXC.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.c_int64(n))
         return exc.value, VXC
+
+    def eval_exc_vxc_uks(self, Ps, Pz):
+        """UKS: Ps = P_alpha + P_beta, Pz = P_alpha - P_beta (polarized
+        functional).  Returns (EXC, VXC_s, VXC_z)."""
+        Ps = np.asfortranarray(Ps, dtype=np.float64)
+        Pz = np.asfortranarray(Pz, dtype=np.float64)
+        n = self._nbf()
+        Vs = np.zeros((n, n), order="F")
+        Vz = np.zeros((n, n), order="F")
+        exc = ctypes.c_double()
+        dp = ctypes.POINTER(ctypes.c_double)
+        _call(_L.gauxc_integrator_eval_exc_vxc_uks, self._h, ctypes.c_int64(Ps.shape[0]),
+              ctypes.c_int64(Ps.shape[1]), Ps.ctypes.data_as(dp), ctypes.c_int64(Ps.shape[0]),
+              Pz.ctypes.data_as(dp), ctypes.c_int64(Pz.shape[0]), ctypes.byref(exc),
+              Vs.ctypes.data_as(dp), ctypes.c_int64(n), Vz.ctypes.data_as(dp), ctypes.c_int64(n))
+        return exc.value, Vs, Vz
+
+    def eval_exc_uks(self, Ps, Pz):
+        Ps = np.asfortranarray(Ps, dtype=np.float64)
+        Pz = np.asfortranarray(Pz, dtype=np.float64)
+        exc = ctypes.c_double()
+        dp = ctypes.POINTER(ctypes.c_double)
+        _call(_L.gauxc_integrator_eval_exc_uks, self._h, ctypes.c_int64(Ps.shape[0]),
+              ctypes.c_int64(Ps.shape[1]), Ps.ctypes.data_as(dp), ctypes.c_int64(Ps.shape[0]),
+              Pz.ctypes.data_as(dp), ctypes.c_int64(Pz.shape[0]), ctypes.byref(exc))
+        return exc.value
 
     def eval_exc(self, P):
         P = np.asfortranarray(P, dtype=np.float64)

@@ -97,6 +97,10 @@ PROTOTYPES = {
     "gauxc_integrator_eval_exc_rks": (None, [S, GauXCIntegrator, i64, i64, P(dbl), i64, P(dbl)]),
     "gauxc_integrator_eval_exc_vxc_rks": (None, [S, GauXCIntegrator, i64, i64, P(dbl), i64,
                                                  P(dbl), P(dbl), i64]),
+    "gauxc_integrator_eval_exc_uks": (None, [S, GauXCIntegrator, i64, i64, P(dbl), i64, P(dbl),
+                                             i64, P(dbl)]),
+    "gauxc_integrator_eval_exc_vxc_uks": (None, [S, GauXCIntegrator, i64, i64, P(dbl), i64,
+                                                 P(dbl), i64, P(dbl), P(dbl), i64, P(dbl), i64]),
     "gauxc_gb300_version": (ctypes.c_char_p, []),
     "gauxc_gb300_device_count": (I, []),
     "gauxc_gb300_basisset_nshells": (sz, [S, GauXCBasisSet]),

@@ -34,6 +34,7 @@ struct XCFunctionalDesc {
   double kappa;    // PBE exchange kappa
   double mu;       // PBE exchange mu
   int is_gga;
+  int polarized = 0;  // spin-polarized (UKS) functional
 };
 
 constexpr double kRhoTolX = 1e-15;

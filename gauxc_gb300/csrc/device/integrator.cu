@@ -81,6 +81,7 @@ struct Batch {
   int coll_begin, coll_end;
   int dens_begin, dens_end;
   int vxc_begin, vxc_end;
+  int64_t g0 = 0, g1 = 0;  // padded point range of the batch's tasks
 };
 
 // One batch of point blocks of the mixed path.
@@ -137,6 +138,9 @@ class DeviceIntegrator {
 
   void eval(const double* P, int64_t ldp, double* VXC, int64_t ldvxc, double* EXC, double* NEL,
             bool den_only);
+  // UKS: Ps = P_a + P_b, Pz = P_a - P_b in, VXC_s / VXC_z out (both null: EXC only).
+  void eval_uks(const double* Ps, int64_t ldps, const double* Pz, int64_t ldpz, double* VXCs,
+                int64_t ldvs, double* VXCz, int64_t ldvz, double* EXC, double* NEL);
   // All device work of one call on this integrator's stream, without waiting:
   // P (host, ld ldp) in, VXC (host, ld ldvxc) out when do_vxc, {EXC, N_el}
   // into en_host and the pipeline error flag into err_host.  Host buffers must
@@ -151,6 +155,15 @@ class DeviceIntegrator {
   void build(const LoadBalancer& lb);
   void build_mixed(const LoadBalancer& lb);
   int64_t eval_mixed_batches(bool do_vxc);
+  int64_t eval_mixed_batches_uks(bool do_vxc);
+  int64_t enqueue_uks(const double* Ps, int64_t ldps, const double* Pz, int64_t ldpz,
+                      double* VXCs, int64_t ldvs, double* VXCz, int64_t ldvz, double* en_host,
+                      int* err_host, bool do_vxc);
+  // brings a caller density matrix in as c P (c a power of two)
+  int64_t load_density(const double* P, int64_t ldp, double* dst, double c);
+  // VXC = A + A^T out to the caller (host_direct_: straight; otherwise staged)
+  int64_t store_vxc(const double* A, double* stage, double* VXC, int64_t ldvxc);
+  void ensure_uks();
 
   XCFunctionalDesc func_;
   Precision prec_;
@@ -177,6 +190,20 @@ class DeviceIntegrator {
   double* A_ = nullptr;
   double* V_ = nullptr;
   double* out_ = nullptr;
+  int64_t npts_plan_ = 0;
+  // UKS work space (first polarized call): the z density, its VXC
+  // accumulator (and staging), (rho, grad rho) of both densities, Z_z
+  // coefficients, P_z row scales, functional partials of the FP64 path
+  bool uks_ready_ = false;
+  double* Pz_ = nullptr;
+  double* Az_ = nullptr;
+  double* Vz_ = nullptr;
+  double* rho4s_ = nullptr;
+  double* rho4z_ = nullptr;
+  double4* zcoefz_ = nullptr;
+  double* prsz_ = nullptr;
+  double2* partials_pol_ = nullptr;
+  int npol_ = 0;
   // mixed path (point blocks)
   PBMaskDev mk_{};
   MixedPBDev mp_{};
@@ -250,6 +277,7 @@ void DeviceIntegrator::build(const LoadBalancer& lb) {
   GB300_CUDA(cudaMemsetAsync(err_, 0, sizeof(int), s));
   if (prec_ == Precision::Mixed) {
     build_mixed(lb);
+    if (func_.polarized) ensure_uks();
     GB300_CUDA(cudaStreamSynchronize(s));
     generation = lb.generation;
     return;
@@ -322,6 +350,7 @@ void DeviceIntegrator::build(const LoadBalancer& lb) {
   GB300_CUDA(cudaMemGetInfo(&free_b, &total_b));
   const double nbf2 = (double)nbf_ * nbf_ * 8.;
   double static_bytes = 3 * nbf2 + pts * (4 * 8. + 32.) + bf_list.size() * 4. + 1e6;
+  if (func_.polarized) static_bytes += 3 * nbf2 + pts * (2 * 32. + 32.);  // ensure_uks
   double budget;
   if (rt_->user_mem)
     budget = (double)rt_->user_bytes - rt_->user_used - static_bytes - 64e6;
@@ -360,6 +389,11 @@ void DeviceIntegrator::build(const LoadBalancer& lb) {
   cur.dens_end = (int)dens.size();
   cur.vxc_end = (int)vx.size();
   if (nt > 0) batches_.push_back(cur);
+  for (Batch& b : batches_) {
+    b.g0 = pt_off[b.t_begin];
+    b.g1 = pt_off[b.t_end - 1] + npts_pad[b.t_end - 1];
+  }
+  npts_plan_ = pts;
   stats.nbatches = (int64_t)batches_.size();
   stats.scratch_bytes = max_used;
 
@@ -386,8 +420,30 @@ void DeviceIntegrator::build(const LoadBalancer& lb) {
   scr_ = arena_.alloc<double>((size_t)(max_used / 8.) + 1);
   zcoef_ = arena_.alloc<double4>(std::max<int64_t>(pts, 1));
   partials_ = arena_.alloc<double2>(std::max(ndens_, 1));
+  if (func_.polarized) ensure_uks();
   GB300_CUDA(cudaStreamSynchronize(s));
   generation = lb.generation;
+}
+
+void DeviceIntegrator::ensure_uks() {
+  if (uks_ready_) return;
+  const size_t n2 = (size_t)nbf_ * nbf_;
+  const size_t np = (size_t)std::max<int64_t>(npts_plan_, 1);
+  Pz_ = arena_.alloc<double>(n2);
+  Az_ = arena_.alloc<double>(n2);
+  if (!host_direct_) Vz_ = arena_.alloc<double>(n2);
+  rho4s_ = prec_ == Precision::Mixed ? rho4_ : arena_.alloc<double>(4 * np);
+  rho4z_ = arena_.alloc<double>(4 * np);
+  zcoefz_ = arena_.alloc<double4>(np);
+  const int nb = prec_ == Precision::Mixed ? (int)mbatches_.size() : (int)batches_.size();
+  npol_ = std::max(nb, 1) * functional_partial_blocks();
+  if (prec_ == Precision::Mixed) {
+    prsz_ = arena_.alloc<double>((size_t)nbf_);
+    partials_pol_ = partials_;  // one block of partials per batch, as the RKS pass
+  } else {
+    partials_pol_ = arena_.alloc<double2>((size_t)npol_);
+  }
+  uks_ready_ = true;
 }
 
 // Padded tensor-core work of one point block: density GEMM (M = basis rows
@@ -517,6 +573,7 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
       member.push_back(0);
     }
     pts += npts_pad[i];
+    npts_plan_ = pts;
     stats.npts += b.npts;
     stats.sum_pad_npts_nbe2 += (double)npts_pad[i] * nu_pad[i] * nu_pad[i];
     {
@@ -545,8 +602,10 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
   // ---- batches under the workspace budget
   size_t free_b = 0, total_b = 0;
   GB300_CUDA(cudaMemGetInfo(&free_b, &total_b));
-  const double static_bytes = pts * (3 * 8. + 8. + 32. + 32. + 4.) + bf_list.size() * 4. +
-                              mask.size() + 64e6;
+  double static_bytes = pts * (3 * 8. + 8. + 32. + 32. + 4.) + bf_list.size() * 4. +
+                        mask.size() + 64e6;
+  if (func_.polarized)  // ensure_uks
+    static_bytes += 3. * nbf_ * nbf_ * 8. + pts * (32. + 32.) + nbf_ * 8.;
   double budget = rt_->user_mem ? (double)rt_->user_bytes - rt_->user_used - static_bytes
                                 : rt_->fill_fraction * (double)free_b - static_bytes;
   if (const char* cap = std::getenv("GAUXC_GB300_SCRATCH_GB")) budget = std::min(budget, atof(cap) * 1e9);
@@ -796,6 +855,204 @@ int64_t DeviceIntegrator::enqueue(const double* P, int64_t ldp, double* VXC, int
   return launches;
 }
 
+int64_t DeviceIntegrator::load_density(const double* P, int64_t ldp, double* dst, double c) {
+  cudaStream_t s = stream_;
+  const size_t row = (size_t)nbf_ * sizeof(double);
+  int64_t n = 0;
+  if (host_direct_) {
+    launch_copy_matrix(P, ldp, dst, nbf_, nbf_, s);
+    ++n;
+  } else if (ldp == nbf_) {
+    GB300_CUDA(cudaMemcpyAsync(dst, P, row * nbf_, cudaMemcpyHostToDevice, s));
+  } else {
+    GB300_CUDA(cudaMemcpy2DAsync(dst, row, P, (size_t)ldp * sizeof(double), row, nbf_,
+                                 cudaMemcpyHostToDevice, s));
+  }
+  if (c != 1.) {
+    launch_scale(dst, (int64_t)nbf_ * nbf_, c, s);
+    ++n;
+  }
+  return n;
+}
+
+int64_t DeviceIntegrator::store_vxc(const double* A, double* stage, double* VXC, int64_t ldvxc) {
+  cudaStream_t s = stream_;
+  const size_t row = (size_t)nbf_ * sizeof(double);
+  if (host_direct_) {
+    launch_symmetrize(A, nbf_, VXC, ldvxc, s);
+    return 1;
+  }
+  launch_symmetrize(A, nbf_, stage, nbf_, s);
+  if (ldvxc == nbf_)
+    GB300_CUDA(cudaMemcpyAsync(VXC, stage, row * nbf_, cudaMemcpyDeviceToHost, s));
+  else
+    GB300_CUDA(cudaMemcpy2DAsync(VXC, (size_t)ldvxc * sizeof(double), stage, row, row, nbf_,
+                                 cudaMemcpyDeviceToHost, s));
+  return 1;
+}
+
+int64_t DeviceIntegrator::eval_mixed_batches_uks(bool do_vxc) {
+  cudaStream_t s = stream_;
+  int64_t launches = 0;
+  launches += timed(4, [&] {
+    launch_p_row_scales(P_, nbf_, prs_, s);
+    launch_p_row_scales(Pz_, nbf_, prsz_, s);
+    return (int64_t)2;
+  });
+  for (const MBatch& b : mbatches_) {
+    const size_t bytes = (size_t)(b.g1 - b.g0) * 4 * sizeof(double);
+    GB300_CUDA(cudaMemsetAsync(rho4s_ + 4 * b.g0, 0, bytes, s));
+    GB300_CUDA(cudaMemsetAsync(rho4z_ + 4 * b.g0, 0, bytes, s));
+    launches += timed(0, [&] {
+      launch_collocation_masked(sh_, tk_, mk_, coll_items_ + b.coll_begin,
+                                b.coll_end - b.coll_begin, f64_, gga_, s);
+      return (int64_t)1;
+    });
+    launches += timed(5, [&] {
+      launch_phi_digits(tk_, mp_, b.b0, b.b1, gga_, f64_, dig_, s);
+      return (int64_t)1;
+    });
+    const OzSchedule xs{slots_, sched_ + b.x_sched, b.x_ncl, wait_ns, withhold ? 1 : 0};
+    // the two densities in turn through the same P digit space
+    for (int d = 0; d < 2; ++d) {
+      launches += timed(6, [&] {
+        launch_p_digits(tk_, mp_, b.b0, b.b1, b.max_nu_pad, gga_, d ? Pz_ : P_, d ? prsz_ : prs_,
+                        nbf_, f64_, dig_, s);
+        return (int64_t)1;
+      });
+      launches += timed(1, [&] {
+        launch_ozaki_x(tk_, mp_, xs, f64_, dig_, gga_, d ? rho4z_ : rho4s_, err_, s);
+        return (int64_t)1;
+      });
+    }
+    launches += timed(4, [&] {
+      launch_functional_pol(b.g0, b.g1, tk_.w, rho4s_, rho4z_, func_, zcoef_, zcoefz_,
+                            partials_pol_ + b.partial_base, true, s);
+      return (int64_t)1;
+    });
+    if (!do_vxc) continue;
+    const OzSchedule vs{slots_, sched_ + b.v_sched, b.v_ncl, wait_ns, withhold ? 1 : 0};
+    for (int d = 0; d < 2; ++d) {
+      launches += timed(2, [&] {
+        launch_z_digits(tk_, mp_, b.b0, b.b1, zoff_h_[b.b0], zoff_h_[b.b1], gga_,
+                        d ? zcoefz_ : zcoef_, f64_, dig_, s);
+        return (int64_t)2;
+      });
+      launches += timed(3, [&] {
+        launch_ozaki_v(tk_, mp_, vs, f64_, dig_, gga_, d ? Az_ : A_, nbf_, err_, s);
+        return (int64_t)1;
+      });
+    }
+  }
+  return launches;
+}
+
+int64_t DeviceIntegrator::enqueue_uks(const double* Ps, int64_t ldps, const double* Pz,
+                                      int64_t ldpz, double* VXCs, int64_t ldvs, double* VXCz,
+                                      int64_t ldvz, double* en_host, int* err_host, bool do_vxc) {
+  ensure_uks();
+  cudaStream_t s = stream_;
+  GB300_CUDA(cudaMemsetAsync(err_, 0, sizeof(int), s));
+  GB300_CUDA(cudaEventRecord(ev_[0], s));
+  // P_s / 2 and P_z / 2: the RKS passes (X = 2 P phi) then give X = P phi
+  int64_t launches = load_density(Ps, ldps, P_, 0.5) + load_density(Pz, ldpz, Pz_, 0.5);
+  GB300_CUDA(cudaEventRecord(ev_[1], s));
+  if (do_vxc) {
+    GB300_CUDA(cudaMemsetAsync(A_, 0, (size_t)nbf_ * nbf_ * sizeof(double), s));
+    GB300_CUDA(cudaMemsetAsync(Az_, 0, (size_t)nbf_ * nbf_ * sizeof(double), s));
+  }
+  pev_used_ = 0;
+  if (prec_ == Precision::Mixed) {
+    launches += eval_mixed_batches_uks(do_vxc);
+  } else {
+    const int nfb = functional_partial_blocks();
+    for (size_t ib = 0; ib < batches_.size(); ++ib) {
+      const Batch& b = batches_[ib];
+      const int nt = b.t_end - b.t_begin;
+      launches += timed(0, [&] {
+        launch_collocation(sh_, tk_, coll_items_ + b.coll_begin, b.coll_end - b.coll_begin, scr_,
+                           gga_, s);
+        return (int64_t)1;
+      });
+      launches += timed(1, [&] {
+        launch_density_fp64_rho(tk_, dens_items_ + b.dens_begin, b.dens_end - b.dens_begin, scr_,
+                                P_, nbf_, gga_, reinterpret_cast<double4*>(rho4s_), s);
+        launch_density_fp64_rho(tk_, dens_items_ + b.dens_begin, b.dens_end - b.dens_begin, scr_,
+                                Pz_, nbf_, gga_, reinterpret_cast<double4*>(rho4z_), s);
+        return (int64_t)2;
+      });
+      launches += timed(4, [&] {
+        launch_functional_pol(b.g0, b.g1, tk_.w, rho4s_, rho4z_, func_, zcoef_, zcoefz_,
+                              partials_pol_ + ib * nfb, false, s);
+        return (int64_t)1;
+      });
+      if (!do_vxc) continue;
+      for (int d = 0; d < 2; ++d) {
+        launches += timed(2, [&] {
+          launch_zmat(tk_, b.t_begin, nt, d ? zcoefz_ : zcoef_, scr_, gga_, s);
+          return (int64_t)1;
+        });
+        launches += timed(3, [&] {
+          launch_vxc_fp64(tk_, vxc_items_ + b.vxc_begin, b.vxc_end - b.vxc_begin, scr_,
+                          d ? Az_ : A_, nbf_, gga_, s);
+          return (int64_t)1;
+        });
+      }
+    }
+  }
+  launches += timed(4, [&] {
+    launch_reduce_partials(partials_pol_, npol_, out_, s);
+    return (int64_t)1;
+  });
+  GB300_CUDA(cudaEventRecord(ev_[2], s));
+  if (do_vxc) {
+    launches += store_vxc(A_, V_, VXCs, ldvs);
+    launches += store_vxc(Az_, Vz_, VXCz, ldvz);
+  }
+  GB300_CUDA(cudaMemcpyAsync(en_host, out_, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GB300_CUDA(cudaMemcpyAsync(err_host, err_, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GB300_CUDA(cudaEventRecord(ev_[3], s));
+  stats.gpu_launches = launches;
+  return launches;
+}
+
+void DeviceIntegrator::eval_uks(const double* Ps, int64_t ldps, const double* Pz, int64_t ldpz,
+                                double* VXCs, int64_t ldvs, double* VXCz, int64_t ldvz,
+                                double* EXC, double* NEL) {
+  auto t_host0 = std::chrono::steady_clock::now();
+  const bool do_vxc = VXCs != nullptr && VXCz != nullptr;
+  double en[2] = {0., 0.};
+  int herr = 0;
+  const int64_t launches =
+      enqueue_uks(Ps, ldps, Pz, ldpz, VXCs, ldvs, VXCz, ldvz, en, &herr, do_vxc);
+  GB300_CUDA(cudaStreamSynchronize(stream_));
+  if (herr)
+    throw error("a tensor-core pipeline wait expired on the device (error code " +
+                std::to_string(herr) + ")");
+  auto t_host1 = std::chrono::steady_clock::now();
+  if (EXC) *EXC = en[0];
+  if (NEL) *NEL = en[1];
+  float h2d, comp, d2h;
+  GB300_CUDA(cudaEventElapsedTime(&h2d, ev_[0], ev_[1]));
+  GB300_CUDA(cudaEventElapsedTime(&comp, ev_[1], ev_[2]));
+  GB300_CUDA(cudaEventElapsedTime(&d2h, ev_[2], ev_[3]));
+  timings["h2d_ms"] = h2d;
+  timings["compute_ms"] = comp;
+  timings["d2h_ms"] = d2h;
+  timings["wall_ms"] = std::chrono::duration<double, std::milli>(t_host1 - t_host0).count();
+  timings["gpu_launches"] = (double)launches;
+  for (int k = 0; k < 7; ++k) {
+    kclass_ms[k] = 0.;
+    kclass_n[k] = 0;
+  }
+  for (size_t i = 0; i < pev_used_; i += 2) {
+    float ms = 0.f;
+    GB300_CUDA(cudaEventElapsedTime(&ms, pev_[i], pev_[i + 1]));
+    kclass_ms[pev_class_[i]] += ms;
+    kclass_n[pev_class_[i]] += pev_class_[i + 1];
+  }
+}
+
 void DeviceIntegrator::eval(const double* P, int64_t ldp, double* VXC, int64_t ldvxc, double* EXC,
                             double* NEL, bool den_only) {
   auto t_host0 = std::chrono::steady_clock::now();
@@ -857,11 +1114,30 @@ void check_dims(const XCIntegratorHandle& h, int64_t m, int64_t n, int64_t ldp) 
 void integrator_eval_exc_vxc(XCIntegratorHandle& h, int64_t m, int64_t n, const double* P,
                              int64_t ldp, double* VXC, int64_t ldvxc, double* EXC) {
   if (!P) throw error("null density matrix");
+  if (h.func->polarized) throw error("RKS evaluation requires an unpolarized functional");
   check_dims(h, m, n, ldp);
   if (VXC && ldvxc < h.lb->basis->nbf) throw error("Invalid LDVXC");
   ensure_plan(h);
   double nel = 0.;
   h.dev->eval(P, ldp, VXC, ldvxc, EXC, &nel, false);
+  h.last_exc = EXC ? *EXC : 0.;
+  h.last_nel = nel;
+}
+
+void integrator_eval_exc_vxc_uks(XCIntegratorHandle& h, int64_t m, int64_t n, const double* Ps,
+                                 int64_t ldps, const double* Pz, int64_t ldpz, double* VXCs,
+                                 int64_t ldvs, double* VXCz, int64_t ldvz, double* EXC) {
+  if (!Ps || !Pz) throw error("null density matrix");
+  if (!h.func->polarized) throw error("UKS evaluation requires a polarized functional");
+  check_dims(h, m, n, ldps);
+  check_dims(h, m, n, ldpz);
+  if ((VXCs == nullptr) != (VXCz == nullptr))
+    throw error("VXC_s and VXC_z must both be given (or both be null for EXC only)");
+  const int64_t nbf = h.lb->basis->nbf;
+  if (VXCs && (ldvs < nbf || ldvz < nbf)) throw error("Invalid LDVXC");
+  ensure_plan(h);
+  double nel = 0.;
+  h.dev->eval_uks(Ps, ldps, Pz, ldpz, VXCs, ldvs, VXCz, ldvz, EXC, &nel);
   h.last_exc = EXC ? *EXC : 0.;
   h.last_nel = nel;
 }
@@ -973,8 +1249,11 @@ class IntegratorBatch {
  public:
   explicit IntegratorBatch(const std::vector<XCIntegratorHandle*>& hs) : hs_(hs) {
     if (hs_.empty()) throw error("empty integrator batch");
-    for (auto* h : hs_)
+    for (auto* h : hs_) {
       if (!h) throw error("null integrator in batch");
+      if (h->func && h->func->polarized)
+        throw error("batched evaluation takes RKS members (unpolarized functionals) only");
+    }
     // Members share the device: each one without its own work-space cap gets
     // an equal share of the memory free now (plus what its current plan holds).
     size_t free_b = 0, total_b = 0;

@@ -217,7 +217,7 @@ void collocation_device(const BasisSet& bs, int64_t npts, const double* points, 
 }
 
 // ---------------------------------------------------------------- functionals
-std::shared_ptr<XCFunctionalDesc> make_functional(const std::string& name0) {
+std::shared_ptr<XCFunctionalDesc> make_functional(const std::string& name0, bool polarized) {
   std::string name = name0;
   for (auto& ch : name) ch = (char)toupper(ch);
   auto f = std::make_shared<XCFunctionalDesc>();
@@ -242,6 +242,7 @@ std::shared_ptr<XCFunctionalDesc> make_functional(const std::string& name0) {
   } else {
     throw error("functional not supported by this build: " + name0);
   }
+  f->polarized = polarized ? 1 : 0;
   return f;
 }
 

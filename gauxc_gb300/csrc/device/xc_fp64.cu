@@ -30,13 +30,17 @@ namespace {
 constexpr int TM = 64, TN = 64, KT = 16, NT = 256;
 
 // ---------------------------------------------------------------- density
-template <bool GGA>
+// RHO: write (rho, grad rho) of each point to rho_out instead of evaluating
+// the functional (the two densities of a UKS call, whose polarized
+// functional runs afterwards on both).
+template <bool GGA, bool RHO>
 __global__ void __launch_bounds__(NT) density_fp64_kernel(TasksDev tk, const int2* __restrict__ items,
                                                           const double* __restrict__ scr,
                                                           const double* __restrict__ P, int nbf,
                                                           XCFunctionalDesc func,
                                                           double4* __restrict__ zcoef,
-                                                          double2* __restrict__ partials) {
+                                                          double2* __restrict__ partials,
+                                                          double4* __restrict__ rho_out) {
   __shared__ double As[KT][TM + 1];
   __shared__ double Bs[KT][TN + 1];
   __shared__ double red[2][NT / 16];
@@ -121,6 +125,17 @@ __global__ void __launch_bounds__(NT) density_fp64_kernel(TasksDev tk, const int
     }
   }
 
+  if (RHO) {
+    if (tx == 0) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int64_t g = tk.pt_off[t] + p0 + ty + 16 * i;
+        rho_out[g] = GGA ? make_double4(2. * rho[i], 4. * gx[i], 4. * gy[i], 4. * gz[i])
+                         : make_double4(2. * rho[i], 0., 0., 0.);
+      }
+    }
+    return;
+  }
   double exc_loc = 0., nel_loc = 0.;
   if (tx == 0) {
 #pragma unroll
@@ -246,9 +261,24 @@ void launch_density_fp64(const TasksDev& tk, const int2* items, int nitems, cons
                          double2* partials, cudaStream_t s) {
   if (!nitems) return;
   if (f.is_gga)
-    density_fp64_kernel<true><<<nitems, NT, 0, s>>>(tk, items, scr, P, nbf, f, zcoef, partials);
+    density_fp64_kernel<true, false>
+        <<<nitems, NT, 0, s>>>(tk, items, scr, P, nbf, f, zcoef, partials, nullptr);
   else
-    density_fp64_kernel<false><<<nitems, NT, 0, s>>>(tk, items, scr, P, nbf, f, zcoef, partials);
+    density_fp64_kernel<false, false>
+        <<<nitems, NT, 0, s>>>(tk, items, scr, P, nbf, f, zcoef, partials, nullptr);
+  GB300_CUDA(cudaGetLastError());
+}
+
+void launch_density_fp64_rho(const TasksDev& tk, const int2* items, int nitems, const double* scr,
+                             const double* P, int nbf, bool gga, double4* rho4, cudaStream_t s) {
+  if (!nitems) return;
+  XCFunctionalDesc f{};
+  if (gga)
+    density_fp64_kernel<true, true>
+        <<<nitems, NT, 0, s>>>(tk, items, scr, P, nbf, f, nullptr, nullptr, rho4);
+  else
+    density_fp64_kernel<false, true>
+        <<<nitems, NT, 0, s>>>(tk, items, scr, P, nbf, f, nullptr, nullptr, rho4);
   GB300_CUDA(cudaGetLastError());
 }
 

@@ -8,6 +8,21 @@ namespace gb300 {
 void launch_density_fp64(const TasksDev& tk, const int2* items, int nitems, const double* scr,
                          const double* P, int nbf, const XCFunctionalDesc& f, double4* zcoef,
                          double2* partials, cudaStream_t s);
+// (rho, grad rho) of every point of the items into rho4 (no functional): the
+// per-density pass of a UKS call.
+void launch_density_fp64_rho(const TasksDev& tk, const int2* items, int nitems, const double* scr,
+                             const double* P, int nbf, bool gga, double4* rho4, cudaStream_t s);
+// Polarized functional on points [g0, g1) from the (rho, grad rho) of the
+// scalar density Ps and the z density Pz (rho4s, rho4z, 4 doubles a point):
+// the Z coefficients of Z_s and Z_z (FP64 double4, or float-float pairs for
+// the tensor-core path when ff) and functional_partial_blocks() EXC / N_el
+// partials.
+void launch_functional_pol(int64_t g0, int64_t g1, const double* w, const double* rho4s,
+                           const double* rho4z, const XCFunctionalDesc& f, double4* zs,
+                           double4* zz, double2* partials, bool ff, cudaStream_t s);
+// x[i] *= c for n doubles (device memory).
+void launch_scale(double* x, int64_t n, double c, cudaStream_t s);
+
 void launch_zmat(const TasksDev& tk, int t_begin, int ntasks, const double4* zcoef, double* scr,
                  bool gga, cudaStream_t s);
 void launch_vxc_fp64(const TasksDev& tk, const int4* items, int nitems, const double* scr,

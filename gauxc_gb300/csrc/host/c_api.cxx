@@ -433,12 +433,8 @@ GauXCFunctional gauxc_functional_from_string(GauXCStatus* status, const char* sp
     status_fail(status, "functional string cannot be null");
     return h;
   }
-  if (polarized) {
-    status_fail(status, "spin-polarized functionals are not supported by this build");
-    return h;
-  }
   guarded(status, [&] {
-    h = make_handle<GauXCFunctional>(GauXC_Type_Functional, make_functional(spec));
+    h = make_handle<GauXCFunctional>(GauXC_Type_Functional, make_functional(spec, polarized));
   });
   return h;
 }
@@ -566,6 +562,36 @@ void gauxc_integrator_eval_exc_vxc_rks(GauXCStatus* status, const GauXCIntegrato
   guarded(status, [&] {
     integrator_eval_exc_vxc(*deref<XCIntegratorHandle>(integrator.ptr), m, n, P, ldp, vxc, vxc_ld,
                             exc);
+  });
+}
+
+void gauxc_integrator_eval_exc_uks(GauXCStatus* status, const GauXCIntegrator integrator,
+                                   const int64_t m, const int64_t n, const double* Ps,
+                                   const int64_t ldps, const double* Pz, const int64_t ldpz,
+                                   double* exc) {
+  status_init(status);
+  if (!check(status, integrator, GauXC_Type_Integrator, "Integrator")) return;
+  if (!Ps || !Pz) return status_fail(status, "Density matrix pointer cannot be null");
+  if (!exc) return status_fail(status, "Exc output pointer cannot be null");
+  guarded(status, [&] {
+    integrator_eval_exc_vxc_uks(*deref<XCIntegratorHandle>(integrator.ptr), m, n, Ps, ldps, Pz,
+                                ldpz, nullptr, 0, nullptr, 0, exc);
+  });
+}
+
+void gauxc_integrator_eval_exc_vxc_uks(GauXCStatus* status, const GauXCIntegrator integrator,
+                                       const int64_t m, const int64_t n, const double* Ps,
+                                       const int64_t ldps, const double* Pz, const int64_t ldpz,
+                                       double* exc, double* vxcs, const int64_t ldvxcs,
+                                       double* vxcz, const int64_t ldvxcz) {
+  status_init(status);
+  if (!check(status, integrator, GauXC_Type_Integrator, "Integrator")) return;
+  if (!Ps || !Pz) return status_fail(status, "Density matrix pointer cannot be null");
+  if (!exc) return status_fail(status, "Exc output pointer cannot be null");
+  if (!vxcs || !vxcz) return status_fail(status, "VXC matrix pointer cannot be null");
+  guarded(status, [&] {
+    integrator_eval_exc_vxc_uks(*deref<XCIntegratorHandle>(integrator.ptr), m, n, Ps, ldps, Pz,
+                                ldpz, vxcs, ldvxcs, vxcz, ldvxcz, exc);
   });
 }
 

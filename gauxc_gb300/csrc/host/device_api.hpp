@@ -67,6 +67,11 @@ void integrator_eval_exc_vxc(XCIntegratorHandle& h, int64_t m, int64_t n, const 
                              int64_t ldp, double* VXC, int64_t ldvxc, double* EXC);
 void integrator_integrate_den(XCIntegratorHandle& h, int64_t m, int64_t n, const double* P,
                               int64_t ldp, double* NEL);
+// UKS: Ps = P_a + P_b, Pz = P_a - P_b; VXC_s and VXC_z both given, or both null
+// (EXC only).  Needs a polarized functional.  Throws gb300::error.
+void integrator_eval_exc_vxc_uks(XCIntegratorHandle& h, int64_t m, int64_t n, const double* Ps,
+                                 int64_t ldps, const double* Pz, int64_t ldpz, double* VXCs,
+                                 int64_t ldvs, double* VXCz, int64_t ldvz, double* EXC);
 std::map<std::string, double> integrator_timings(const XCIntegratorHandle& h);
 PlanStats integrator_plan_stats(XCIntegratorHandle& h);
 // Per-kernel-class CUDA-event timing of every launch (collocation, density,
@@ -127,7 +132,7 @@ void collocation_device(const BasisSet& basis, int64_t npts, const double* point
                         const int32_t* shell_list, bool grad, double* phi, double* dphi_x,
                         double* dphi_y, double* dphi_z);
 
-std::shared_ptr<XCFunctionalDesc> make_functional(const std::string& name);
+std::shared_ptr<XCFunctionalDesc> make_functional(const std::string& name, bool polarized = false);
 bool functional_is_gga(const XCFunctionalDesc& f);
 
 int cuda_device_count();

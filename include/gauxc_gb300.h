@@ -14,7 +14,7 @@
  * statistics, per-call timings, N_el of the last call, and stage-level entry
  * points (SSF weights, collocation) that the parity tests call directly.
  *
- * Supported: RKS, LDA/GGA functionals SVWN5, PBE, revPBE, PBE0 (semilocal part),
+ * Supported: RKS and UKS, LDA/GGA functionals SVWN5, PBE, revPBE, PBE0 (semilocal part),
  * Mura-Knowles radial grids with Lebedev angular grids (unpruned, Robust and
  * Treutler pruning), SSF partition weights on the device, shells with l <= 4.
  */
@@ -217,6 +217,21 @@ void gauxc_integrator_eval_exc_vxc_rks(GauXCStatus* status, const GauXCIntegrato
                                        const double* density_matrix, const int64_t ldp,
                                        double* exc, double* vxc_matrix,
                                        const int64_t vxc_ld);                     /* xc_integrator.h:180 */
+
+/* UKS: density_matrix_s = P_alpha + P_beta, density_matrix_z = P_alpha - P_beta;
+   needs a functional made with polarized = true. */
+void gauxc_integrator_eval_exc_uks(GauXCStatus* status, const GauXCIntegrator integrator,
+                                   const int64_t m, const int64_t n,
+                                   const double* density_matrix_s, const int64_t ldp_s,
+                                   const double* density_matrix_z, const int64_t ldp_z,
+                                   double* exc);                                  /* xc_integrator.h:124 */
+void gauxc_integrator_eval_exc_vxc_uks(GauXCStatus* status, const GauXCIntegrator integrator,
+                                       const int64_t m, const int64_t n,
+                                       const double* density_matrix_s, const int64_t ldp_s,
+                                       const double* density_matrix_z, const int64_t ldp_z,
+                                       double* exc, double* vxc_matrix_s, const int64_t vxc_ld_s,
+                                       double* vxc_matrix_z,
+                                       const int64_t vxc_ld_z);                   /* xc_integrator.h:208 */
 
 /* ------------------------------------------------------------------ extensions */
 

@@ -16,7 +16,9 @@
  *       lwd_kernel, reduction_kernel).get_instance(func, lb)
  *                                          include/gauxc/xc_integrator/integrator_factory.hpp:24-111
  *   XCIntegrator<MatrixType>::eval_exc_vxc(P) -> std::tuple<EXC, VXC>,
- *       eval_exc(P), integrate_den(P)     include/gauxc/xc_integrator.hpp:30-94
+ *       eval_exc_vxc(Ps, Pz) -> std::tuple<EXC, VXC_s, VXC_z> (UKS),
+ *       eval_exc(P), eval_exc(Ps, Pz), integrate_den(P)
+ *                                          include/gauxc/xc_integrator.hpp:30-94
  * The classes live in namespace gauxc_gb300 so that they can sit next to the
  * reference headers; a caller switches with one namespace alias.
  *
@@ -308,6 +310,7 @@ class XCIntegrator {
   using matrix_type = MatrixType;
   using value_type = typename MatrixType::value_type;
   using exc_vxc_type_rks = std::tuple<value_type, matrix_type>;
+  using exc_vxc_type_uks = std::tuple<value_type, matrix_type, matrix_type>;
 
   explicit XCIntegrator(GauXCIntegrator h, int64_t nbf) : h_(h), nbf_(nbf) {}
 
@@ -330,6 +333,21 @@ class XCIntegrator {
     detail::call(gauxc_integrator_eval_exc_vxc_rks, h_.get(), (int64_t)P.rows(),
                  (int64_t)P.cols(), P.data(), (int64_t)P.rows(), &e, V.data(), (int64_t)nbf_);
     return exc_vxc_type_rks(e, std::move(V));
+  }
+  // UKS: Ps = P_alpha + P_beta, Pz = P_alpha - P_beta (polarized functional)
+  value_type eval_exc(const MatrixType& Ps, const MatrixType& Pz) {
+    value_type e = 0;
+    detail::call(gauxc_integrator_eval_exc_uks, h_.get(), (int64_t)Ps.rows(), (int64_t)Ps.cols(),
+                 Ps.data(), (int64_t)Ps.rows(), Pz.data(), (int64_t)Pz.rows(), &e);
+    return e;
+  }
+  exc_vxc_type_uks eval_exc_vxc(const MatrixType& Ps, const MatrixType& Pz) {
+    MatrixType Vs(nbf_, nbf_), Vz(nbf_, nbf_);
+    value_type e = 0;
+    detail::call(gauxc_integrator_eval_exc_vxc_uks, h_.get(), (int64_t)Ps.rows(),
+                 (int64_t)Ps.cols(), Ps.data(), (int64_t)Ps.rows(), Pz.data(), (int64_t)Pz.rows(),
+                 &e, Vs.data(), (int64_t)nbf_, Vz.data(), (int64_t)nbf_);
+    return exc_vxc_type_uks(e, std::move(Vs), std::move(Vz));
   }
   const GauXCIntegrator& handle() const { return h_.get(); }
 

@@ -149,3 +149,22 @@ def test_null_status_raises_like_the_reference(g):
     assert L.gauxc_molecule_natoms(None, m) == 0
     L.gauxc_molecule_delete(None, ctypes.byref(m))
     assert not m.ptr
+
+
+def test_spin_mismatch_errors(g):
+    from gauxc_gb300 import workloads as W
+    from gauxc_gb300._capi import GauXCError
+    s = W.config(0)["systems"][0]
+    mol, basis, mg, lb = W.build_system(s, device=False)
+    f = g.XCIntegratorFactory(g.ExecutionSpace.Device)
+    rks = f.get_instance(g.functional_type("SVWN5"), lb)
+    uks = f.get_instance(g.functional_type("SVWN5", True), lb)
+    P = s["P"]
+    with pytest.raises(GauXCError, match="requires a polarized functional"):
+        rks.eval_exc_vxc_uks(P, P)
+    with pytest.raises(GauXCError, match="requires an unpolarized functional"):
+        uks.eval_exc_vxc(P)
+    with pytest.raises(GauXCError, match="Invalid LDP"):
+        uks.eval_exc_vxc_uks(P, np.zeros((3, 3)))
+    with pytest.raises(GauXCError, match="Same Dimension"):
+        uks.eval_exc_vxc_uks(np.zeros((3, 3)), np.zeros((3, 3)))

@@ -58,3 +58,60 @@ def test_device_functional_matches_oracle(devxc, name):
         # correlation terms; only the regular range is compared
         m = rho > 1e-10
         np.testing.assert_allclose(vs[m], s2[m], rtol=1e-9, atol=1e-300)
+
+
+HARNESS_POL = r"""
+#define GB300_HD
+#include "functionals_pol.cuh"
+extern "C" void dev_xc_pol(int kind, double xs, double cs, double kappa, double mu, int gga,
+                           long n, const double* rho, const double* sigma, double* eps,
+                           double* vr, double* vs) {
+  gb300::XCFunctionalDesc f{kind, xs, cs, kappa, mu, gga};
+  for (long i = 0; i < n; ++i)
+    gb300::xc_eval_pol(f, rho[2 * i], rho[2 * i + 1], sigma[3 * i], sigma[3 * i + 1],
+                       sigma[3 * i + 2], eps[i], vr + 2 * i, vs + 3 * i);
+}
+"""
+
+
+@pytest.fixture(scope="module")
+def devxc_pol():
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    inc = os.path.join(root, "gauxc_gb300", "csrc", "device")
+    d = tempfile.mkdtemp()
+    src = os.path.join(d, "hp.cpp")
+    so = os.path.join(d, "hp.so")
+    open(src, "w").write(HARNESS_POL)
+    subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I", inc, src, "-o", so],
+                   check=True)
+    return ctypes.CDLL(so)
+
+
+@pytest.mark.parametrize("name", ["SVWN5", "PBE", "REVPBE", "PBE0"])
+def test_device_polarized_functional_matches_oracle(devxc_pol, name):
+    """functionals_pol.cuh (host build) against the oracle's polarized
+    functionals over spin polarizations from closed shell to fully polarized."""
+    rng = np.random.default_rng(9)
+    n = 3000
+    rho = 10 ** rng.uniform(-9, 3, n)
+    zeta = np.concatenate([rng.uniform(-1, 1, n - 4), [0.0, 1.0, -1.0, 0.999999]])
+    ra, rb = 0.5 * rho * (1 + zeta), 0.5 * rho * (1 - zeta)
+    c = 4.0 * (3 * np.pi ** 2) ** (2 / 3)
+    saa = rng.uniform(0, 4, n) ** 2 * c * (2 * ra) ** (8 / 3) / 4
+    sbb = rng.uniform(0, 4, n) ** 2 * c * (2 * rb) ** (8 / 3) / 4
+    sab = rng.uniform(-1, 1, n) * np.sqrt(saa * sbb)
+    R = np.ascontiguousarray(np.stack([ra, rb], 1))
+    S = np.ascontiguousarray(np.stack([saa, sab, sbb], 1))
+    kind, xs, cs, kappa, mu, gga = oracle.FUNCTIONALS[name]
+    eps, vr, vs = np.zeros(n), np.zeros((n, 2)), np.zeros((n, 3))
+    dp = ctypes.POINTER(ctypes.c_double)
+    devxc_pol.dev_xc_pol(kind, ctypes.c_double(xs), ctypes.c_double(cs), ctypes.c_double(kappa),
+                         ctypes.c_double(mu), gga, ctypes.c_long(n), R.ctypes.data_as(dp),
+                         S.ctypes.data_as(dp), eps.ctypes.data_as(dp), vr.ctypes.data_as(dp),
+                         vs.ctypes.data_as(dp))
+    e2, v2, s2 = oracle.functional_pol(name, R, S if gga else None)
+    np.testing.assert_allclose(eps, e2, rtol=1e-12, atol=1e-300)
+    np.testing.assert_allclose(vr, v2, rtol=1e-10, atol=1e-300)
+    if gga:
+        m = rho > 1e-8
+        np.testing.assert_allclose(vs[m], s2[m], rtol=1e-9, atol=1e-300)
