@@ -448,12 +448,13 @@ void DeviceIntegrator::ensure_uks() {
 
 // Padded tensor-core work of one point block: density GEMM (M = basis rows
 // padded to kMTile, N = points padded to kNTile, K = basis padded to kBK)
-// plus the symmetric VXC GEMM (about half the M x N basis tiles, K = 2 points).
+// plus the symmetric VXC GEMM (about half the M x N basis tiles, K = 2 points
+// padded to kBK).
 static double pb_cost(int npts, int nu, double nu2_weight) {
-  const double np = (double)round_up(npts, kNTile);
+  const double np = (double)round_up(npts, kNTile), nk = (double)round_up(npts, kBK);
   const double m = (double)round_up(nu, kMTile), n = (double)round_up(nu, kNTile),
                k = (double)round_up(nu, kBK);
-  return m * np * k + m * n * np + nu2_weight * m * n;
+  return m * np * k + m * n * nk + nu2_weight * m * n;
 }
 
 // Point blocks for the tensor-core path: consecutive tasks of one parent atom
@@ -523,8 +524,8 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
   const int npb = (int)pbs.size();
   std::vector<int64_t> pt_off(npb), bf_off(npb), sh_off(npb), f64_off(npb), dig_off(npb),
       mask_off(npb);
-  std::vector<int> npts_pad(npb), nu(npb), nu_pad(npb), nsh(npb), bf_list, sh_list, sh_col,
-      member;
+  std::vector<int> npts_pad(npb), nk(npb), nu(npb), nu_pad(npb), nsh(npb), bf_list, sh_list,
+      sh_col, member;
   std::vector<uint8_t> mask;
   std::vector<double> X, Y, Z, W;
   stats = PlanStats{};
@@ -533,6 +534,7 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
     const PB& b = pbs[order[i]];
     pt_off[i] = pts;
     npts_pad[i] = (int)round_up(b.npts, kNTile);
+    nk[i] = (int)round_up(b.npts, kBK);  // the VXC GEMM's points: real ones, K granularity
     nu[i] = b.nu;
     nu_pad[i] = (int)round_up(b.nu, kMTile);
     nsh[i] = (int)b.shells.size();
@@ -579,17 +581,17 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
     {
       // algorithmic bytes of each kernel at this plan's sizes: phi as
       // float-float pairs (8 B), digit operands 6 BF16 planes (12 B)
-      const PBDims d(npts_pad[i], nu[i]);
+      const PBDims d(npts_pad[i], nu[i], nk[i]);
       const double nq = gga_ ? 4. : 1.;
       const double phi = 8. * d.np * d.nu128;
       stats.kbytes[0] += nq * phi;                                          // collocation
-      stats.kbytes[5] += phi + 12. * ((double)d.nu128 * d.np + (double)d.nun * d.np +
+      stats.kbytes[5] += phi + 12. * ((double)d.nu128 * d.nk + (double)d.nun * d.nk +
                                       (double)d.np * d.nu16);               // phi digits
       stats.kbytes[6] += 8. * d.nu * d.nu + 12. * d.nu128 * d.nu16;         // P digits
       stats.kbytes[1] += 12. * ((double)d.nu128 * d.nu16 + (double)d.np * d.nu16) + nq * phi +
                          32. * d.np;                                        // density GEMM
-      stats.kbytes[2] += nq * phi + 32. * d.np + 12. * (double)(d.nu128 + d.nun) * d.np;  // Z digits
-      stats.kbytes[3] += 12. * (double)(d.nu128 + d.nun) * 2. * d.np + 8. * d.nu * d.nu;  // VXC GEMM
+      stats.kbytes[2] += nq * phi + 32. * d.np + 12. * (double)(d.nu128 + d.nun) * d.nk;  // Z digits
+      stats.kbytes[3] += 12. * (double)(d.nu128 + d.nun) * 2. * d.nk + 8. * d.nu * d.nu;  // VXC GEMM
     }
   }
   for (const auto& t : tasks) {
@@ -626,7 +628,7 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
   };
   for (int i = 0; i < npb; ++i) {
     const double nf = (double)mixed_f64_doubles(npts_pad[i], nu[i], gga_) * 8.;
-    const double nd = (double)mixed_dig_elems(npts_pad[i], nu[i]) * 2.;
+    const double nd = (double)mixed_dig_elems(npts_pad[i], nu[i], nk[i]) * 2.;
     if (nf + nd > budget) throw error("insufficient device memory for one point block");
     if (f64_used + dig_used + nf + nd > budget && i > cur.b0) {
       close_batch(i);
@@ -642,7 +644,7 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
     max_dig = std::max(max_dig, dig_used);
     cur.max_nu_pad = std::max(cur.max_nu_pad, nu_pad[i]);
     for (int b = 0; b < (npts_pad[i] + 127) / 128; ++b) coll.push_back(make_int2(i, b));
-    const PBDims d(npts_pad[i], nu[i]);
+    const PBDims d(npts_pad[i], nu[i], nk[i]);
     // Density tiles in cluster-slot order: the (m0, n0) tiles ("chains") in
     // row-major order, four per block (the last block of a point block
     // padded with empty entries); a block runs its chains' K chunks in
@@ -669,7 +671,7 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
     for (int m0 = 0; m0 < d.nu128; m0 += kMTile)
       for (int n0 = 0; n0 < d.nun; n0 += kNTile)
         if (m0 < n0 + kNTile) {
-          vi.push_back(OzItem{i, m0, n0, 0, 2 * d.np, 0, 0});
+          vi.push_back(OzItem{i, m0, n0, 0, 2 * d.nk, 0, 0});
           oz_set_operands(vi.back(), d, dig_off[i], true);
         }
   }
@@ -717,12 +719,13 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
   mk_.mask = arena_.upload(mask, s);
   mp_.f64_off = tk_.scr_off;
   mp_.dig_off = arena_.upload(dig_off, s);
-  // z_digits CTAs: nu128 np / 2048 per block (256 threads, 8 points each)
+  // z_digits CTAs: nu128 nk / 2048 per block (256 threads, 8 points each)
   zoff_h_.assign(npb + 1, 0);
   for (int i = 0; i < npb; ++i) {
-    const PBDims d(npts_pad[i], nu[i]);
-    zoff_h_[i + 1] = zoff_h_[i] + d.nu128 * d.np / 2048;
+    const PBDims d(npts_pad[i], nu[i], nk[i]);
+    zoff_h_[i + 1] = zoff_h_[i] + d.nu128 * d.nk / 2048;
   }
+  mp_.nk = arena_.upload(nk, s);
   mp_.zoff = arena_.upload(zoff_h_, s);
   coll_items_ = arena_.upload(coll, s);
   slots_ = arena_.upload(slots, s);

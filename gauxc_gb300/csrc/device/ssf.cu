@@ -125,25 +125,45 @@ __device__ __forceinline__ double warp_max(double v) {
 }
 
 // Cell product P_A at point p over the atoms in the chunk's distance order.
+// The atoms come four at a time: their distances and R_AB^-1 are loaded
+// together before the factors are applied in order, so that four loads are
+// in flight instead of one.
 __device__ __forceinline__ double cell_sorted(int A, int natoms, int64_t p, double h,
                                               const uint64_t* __restrict__ keys,
                                               const double* __restrict__ dist, int ld,
                                               const double* __restrict__ rab_inv, int ld_rab) {
+  constexpr int U = 4;
   const double rA = dist[(int64_t)A * ld + p];
   const double* rinv = rab_inv + (int64_t)A * ld_rab;
   // atoms with d_B >= lim have r_B >= kSSFFar r_A (1 + 1e-9): factor 1
   const double lim = kSSFFar * rA * (1. + 1e-9) + h;
   double ps = 1.;
-  for (int k = 0; k < natoms; ++k) {
-    const uint64_t key = keys[k];
-    if ((double)__uint_as_float((unsigned)(key >> 32)) >= lim) break;
-    const int B = (int)(key & 0xFFFFu);
-    if (B == A) continue;
-    const double mu = (rA - dist[(int64_t)B * ld + p]) * rinv[B];
-    if (mu >= kSSFa) return 0.;
-    if (mu > -kSSFa) {
-      ps *= ssf_s(mu);
-      if (ps <= kSSFTol) break;
+  for (int k = 0; k < natoms; k += U) {
+    int B[U];
+    bool use[U];
+    double rB[U], ri[U];
+    int nv = U;  // entries of this group before the first one at or beyond lim
+#pragma unroll
+    for (int j = 0; j < U; ++j) {
+      const int kk = k + j;
+      const uint64_t key = kk < natoms ? keys[kk] : ~0ull;
+      const bool in = kk < natoms && (double)__uint_as_float((unsigned)(key >> 32)) < lim;
+      if (!in && j < nv) nv = j;
+      B[j] = (int)(key & 0xFFFFu);
+      use[j] = in && j < nv && B[j] != A;
+      rB[j] = use[j] ? dist[(int64_t)B[j] * ld + p] : 0.;
+      ri[j] = use[j] ? rinv[B[j]] : 0.;
+    }
+#pragma unroll
+    for (int j = 0; j < U; ++j) {
+      if (j >= nv) return ps;
+      if (!use[j]) continue;
+      const double mu = (rA - rB[j]) * ri[j];
+      if (mu >= kSSFa) return 0.;
+      if (mu > -kSSFa) {
+        ps *= ssf_s(mu);
+        if (ps <= kSSFTol) return ps;
+      }
     }
   }
   return ps;

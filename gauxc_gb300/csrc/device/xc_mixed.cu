@@ -62,7 +62,7 @@ struct PBView {
   __nv_bfloat16 *Pd, *Fd, *Va, *Vb;
   __device__ PBView(const TasksDev& tk, const MixedPBDev& mp, int b, bool gga, const double* f64c,
                     const __nv_bfloat16* digc)
-      : d(tk.npts_pad[b], tk.nbe[b]), o(d, gga ? 4 : 1) {
+      : d(tk.npts_pad[b], tk.nbe[b], mp.nk[b]), o(d, gga ? 4 : 1) {
     double* base = const_cast<double*>(f64c) + mp.f64_off[b];
     phi = reinterpret_cast<const ffl*>(base);
     r = base + o.r;
@@ -93,7 +93,7 @@ __device__ __forceinline__ unsigned long long row8_max(unsigned long long m,
 }
 
 // ---------------------------------------------------------------- phi digits
-// Va[mu][p] (K < np) and Vb[mu][np + p] (rows mu < nun): one thread per
+// Va[mu][p] (K < nk) and Vb[mu][nk + p] (rows mu < nun): one thread per
 // (mu, 8 points), consecutive threads on consecutive mu.  Fd (rows p, K = mu):
 // thread p of the CTA walks the CTA's share of the basis in groups of 8
 // (kPBMaxPts <= blockDim.x).  The point scales sp come from the collocation
@@ -103,10 +103,10 @@ __global__ void phi_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const doub
   const int b = b0 + blockIdx.y;
   PBView v(tk, mp, b, gga, f64, dig);
   const PBDims& d = v.d;
-  const int k2 = 2 * d.np;
+  const int k2 = 2 * d.nk;
   const int stride = gridDim.x * blockDim.x;
   const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
-  for (int u = t0; u < d.nu128 * (d.np / 8); u += stride) {
+  for (int u = t0; u < d.nu128 * (d.nk / 8); u += stride) {
     const int mu = u % d.nu128, p0 = (u / d.nu128) * 8;
     ffl x[8];
     int es[8];
@@ -120,7 +120,7 @@ __global__ void phi_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const doub
 #pragma unroll
     for (int e = 0; e < 8; ++e) es[e] = exp_of_pow2(v.sp[p0 + e]);
     store_digits8(x, es, v.Va + oz_offset(0, mu, p0, kMTile, k2), kMTile * kBK);
-    if (mu < d.nun) store_digits8(x, es, v.Vb + oz_offset(0, mu, d.np + p0, kNTile, k2), kNTile * kBK);
+    if (mu < d.nun) store_digits8(x, es, v.Vb + oz_offset(0, mu, d.nk + p0, kNTile, k2), kNTile * kBK);
   }
   // Fd: thread (point p, sub-lane sub) takes every nsub-th row group of this
   // CTA's share, so that small blocks keep all threads busy
@@ -246,10 +246,10 @@ __global__ void z_scale_kernel(TasksDev tk, MixedPBDev mp, int b0, const double4
   }
 }
 
-// One thread per (row nu, 8-point group): CTA c of the launch covers pairs
-// 256 (c - zoff[b]) .. +255 of block b (zoff: CTA offsets of the blocks,
-// nu128 np / 2048 each), rows in groups of 8 with the point group next, so
-// that 8 lanes write one 128-byte core matrix.
+// One thread per (row nu, 8-point group of the nk VXC points): CTA c of the
+// launch covers pairs 256 (c - zoff[b]) .. +255 of block b (zoff: CTA
+// offsets of the blocks, nu128 nk / 2048 each), rows in groups of 8 with the
+// point group next, so that 8 lanes write one 128-byte core matrix.
 __global__ void __launch_bounds__(256, 4) z_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, int b1, int c0,
                                 const double4* __restrict__ zc, double* f64, __nv_bfloat16* dig,
                                 int gga) {
@@ -262,14 +262,14 @@ __global__ void __launch_bounds__(256, 4) z_digits_kernel(TasksDev tk, MixedPBDe
   const int b = lo;
   PBView v(tk, mp, b, gga, f64, dig);
   const PBDims& d = v.d;
-  const int ng = d.np / 8;
+  const int ng = d.nk / 8;
   const int t = (c - mp.zoff[b]) * blockDim.x + threadIdx.x;
   const int row = (t / (8 * ng)) * 8 + (t & 7), g = (t % (8 * ng)) >> 3;
   if (row >= d.nu128) return;
   // coefficients already scaled by sp (z_scale_kernel): 4 float-float per point
   const float4* zf4 = reinterpret_cast<const float4*>(zc + tk.pt_off[b]) + 2 * (g * 8);
   const int es_z = exp_of_pow2(v.cz[0]);
-  const int k2 = 2 * d.np;
+  const int k2 = 2 * d.nk;
   // Zt in float-float, 16-byte loads: phi of 8 points is 4 float4 per value q
   const float4* f4 = reinterpret_cast<const float4*>(v.phi + (int64_t)row * d.np + g * 8);
   const int64_t qs = v.o.blk / 2;  // one value plane, in float4
@@ -293,7 +293,7 @@ __global__ void __launch_bounds__(256, 4) z_digits_kernel(TasksDev tk, MixedPBDe
   int es[8];
 #pragma unroll
   for (int e = 0; e < 8; ++e) es[e] = es_z;
-  store_digits8(x, es, v.Va + oz_offset(0, row, d.np + g * 8, kMTile, k2), kMTile * kBK);
+  store_digits8(x, es, v.Va + oz_offset(0, row, d.nk + g * 8, kMTile, k2), kMTile * kBK);
   if (row < d.nun) store_digits8(x, es, v.Vb + oz_offset(0, row, g * 8, kNTile, k2), kNTile * kBK);
 }
 

@@ -46,24 +46,26 @@ __host__ __device__ inline int64_t oz_offset(int s, int r, int k, int TR, int kp
   return chunk * TR * kBK + ((rr >> 3) * (kBK / 8) + (kk >> 3)) * 64 + (rr & 7) * 8 + (kk & 7);
 }
 
-// Padded extents of one point block: np points (multiple of kNTile), nu basis
-// functions in the union.
+// Padded extents of one point block: np points (multiple of kNTile: the
+// density GEMM's N tiles and the phi planes), nk <= np points of the VXC
+// GEMM's K extent (the block's real points rounded up to kBK; nk = np when
+// not given), nu basis functions in the union.
 struct PBDims {
-  int np, nu, nu16, nun, nu128;
-  __host__ __device__ PBDims(int np_, int nu_)
+  int np, nu, nu16, nun, nu128, nk;
+  __host__ __device__ PBDims(int np_, int nu_, int nk_ = 0)
       : np(np_), nu(nu_), nu16(oz_round(nu_, kBK)), nun(oz_round(nu_, kNTile)),
-        nu128(oz_round(nu_, kMTile)) {}
+        nu128(oz_round(nu_, kMTile)), nk(nk_ > 0 ? nk_ : np_) {}
   // digit operands (bf16 element offsets within the block's region)
   //   Pd [nu128 rows, TR 128] x [K = mu, nu16]   density GEMM, M operand
   //   Fd [np rows,    TR  64] x [K = mu, nu16]   density GEMM, N operand
-  //   Va [nu128 rows, TR 128] x [K = 2 np]       VXC GEMM, M operand: phi | Z
-  //   Vb [nun rows,   TR  64] x [K = 2 np]       VXC GEMM, N operand: Z | phi
+  //   Va [nu128 rows, TR 128] x [K = 2 nk]       VXC GEMM, M operand: phi | Z
+  //   Vb [nun rows,   TR  64] x [K = 2 nk]       VXC GEMM, N operand: Z | phi
   // so that Va Vb^T = phi^T Z + Z^T phi, the symmetric VXC contribution.
   __host__ __device__ int64_t pd() const { return 0; }
   __host__ __device__ int64_t fd() const { return (int64_t)kSlices * nu128 * nu16; }
   __host__ __device__ int64_t va() const { return fd() + (int64_t)kSlices * np * nu16; }
-  __host__ __device__ int64_t vb() const { return va() + (int64_t)kSlices * nu128 * 2 * np; }
-  __host__ __device__ int64_t dig_elems() const { return vb() + (int64_t)kSlices * nun * 2 * np; }
+  __host__ __device__ int64_t vb() const { return va() + (int64_t)kSlices * nu128 * 2 * nk; }
+  __host__ __device__ int64_t dig_elems() const { return vb() + (int64_t)kSlices * nun * 2 * nk; }
 };
 
 // FP64 region of a point block (offsets in doubles): phi[q][mu][p] (q = value,
@@ -92,7 +94,8 @@ struct PBMaskDev {
 struct MixedPBDev {
   const int64_t* f64_off;   // doubles: PBF64 layout
   const int64_t* dig_off;   // bf16 elements: PBDims layout
-  const int* zoff;          // first z_digits CTA of each block (nu128 np / 2048 per block)
+  const int* zoff;          // first z_digits CTA of each block (nu128 nk / 2048 per block)
+  const int* nk;            // VXC K extent of each block (PBDims::nk)
 };
 
 // One tensor-core GEMM tile: output rows [m0, m0+128) x cols [n0, n0+64),
@@ -107,7 +110,7 @@ struct OzItem {
 // Fills it.a / it.b for a density (vxc false) or VXC (vxc true) tile of a
 // point block with dimensions d whose digits start at element dig_off.
 inline void oz_set_operands(OzItem& it, const PBDims& d, int64_t dig_off, bool vxc) {
-  const int64_t nkb = (vxc ? 2 * d.np : d.nu16) / kBK;
+  const int64_t nkb = (vxc ? 2 * d.nk : d.nu16) / kBK;
   const int64_t kb0 = it.k0 / kBK;
   it.a = dig_off + (vxc ? d.va() : d.pd()) +
          ((int64_t)(it.m0 / kMTile) * nkb + kb0) * (kSlices * kMTile * kBK);
@@ -181,6 +184,6 @@ double ozaki_selftest(int n, int k);
 inline int64_t mixed_f64_doubles(int np, int nu, bool gga) {
   return PBF64(PBDims(np, nu), gga ? 4 : 1).total;
 }
-inline int64_t mixed_dig_elems(int np, int nu) { return PBDims(np, nu).dig_elems(); }
+inline int64_t mixed_dig_elems(int np, int nu, int nk) { return PBDims(np, nu, nk).dig_elems(); }
 
 }  // namespace gb300
