@@ -185,7 +185,7 @@ def host_stats(lb):
     return dict(ntasks=len(infos), npts=sum(i["npts"] for i in infos)), infos
 
 
-def setup_workload(cfg_idx, lwd):
+def setup_workload(cfg_idx, lwd, atom_stride=1):
     import gauxc_gb300 as g
     from gauxc_gb300 import workloads as W
     cfg = W.config(cfg_idx)
@@ -193,6 +193,11 @@ def setup_workload(cfg_idx, lwd):
     t0 = time.perf_counter()
     mol, basis, mg, lb = W.build_system(s)
     t_lb = time.perf_counter() - t0
+    if atom_stride > 1:
+        # the tasks of every atom_stride-th atom: the full system's per-atom
+        # blocks and P gathers on a fraction of the points (profiling case)
+        keep = [i for i in range(lb.ntasks()) if lb.task_info(i)["iParent"] % atom_stride == 0]
+        lb = lb.subset(keep)
     t0 = time.perf_counter()
     mw = g.MolecularWeightsFactory(g.ExecutionSpace.Device).get_instance()
     mw.modify_weights(lb)
@@ -471,6 +476,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=16.0)
     ap.add_argument("--scratch-gb", type=float, default=0.0,
                     help="cap of the plan's work space per pass (0 = from free memory)")
+    ap.add_argument("--atom-stride", type=int, default=1,
+                    help="profiling case: only the tasks of every k-th atom (default: all)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-check", action="store_true",
                     help="mixed path: skip the FP64 device pass used for dEXC / dVXC")
@@ -499,7 +506,7 @@ def main():
         return run_batched(args, ncores)
 
     g.set_device(0)
-    ctx = setup_workload(args.config, args.lwd)
+    ctx = setup_workload(args.config, args.lwd, args.atom_stride)
     integ, s = ctx["integ"], ctx["sys"]
     if args.scratch_gb > 0:
         integ.set_plan_params(scratch_gb=args.scratch_gb)
@@ -627,7 +634,7 @@ def main():
         data="synthetic: seeded water cluster, even-tempered basis, P=CC^T (no dataset)",
         config=config_dict(args.config, [stats], [nbf]),
         path=dict(lwd=args.lwd, parallelism="1 GPU", nbatches=int(stats["nbatches"]),
-                  scratch_gb=stats["scratch_bytes"] / 1e9),
+                  scratch_gb=stats["scratch_bytes"] / 1e9, atom_stride=args.atom_stride),
         e2e=dict(value=e2e, unit="s", h2d_bytes_per_step=nbf * nbf * 8,
                  d2h_bytes_per_step=nbf * nbf * 8 + 16, pinned=pinned,
                  breakdown_ms={k: float(np.mean(v)) for k, v in brk.items()}),

@@ -94,7 +94,7 @@ __global__ void ssf_weights_kernel(int64_t npts, int natoms, const int32_t* __re
 // Same weights, far fewer cell-product factors.  A warp takes 32 consecutive
 // points (a chunk; the points of one task are close together) and
 //   * sorts the atoms by their distance d_B to the centre of the chunk's
-//     bounding box (bitonic sort of (d_B, B) keys in shared memory), h being
+//     bounding box (bitonic sort of 32-bit (d_B, B) keys in shared memory), h being
 //     the chunk's radius, so that every point has r_B in [d_B - h, d_B + h];
 //   * drops, for the whole chunk, every atom A that one of the four atoms
 //     nearest to the centre kills at every point:
@@ -124,46 +124,35 @@ __device__ __forceinline__ double warp_max(double v) {
   return v;
 }
 
+// Sort keys of the chunk's atoms: the float bits of d_B rounded down with the
+// low 11 mantissa bits replaced by the atom index (natoms <= 2048), so that
+// the key orders by distance and the key with the index bits cleared is a
+// lower bound of d_B.
+constexpr uint32_t kSSFIndexMask = 0x7FFu;
+__device__ __forceinline__ double key_dist(uint32_t key) {
+  return (double)__uint_as_float(key & ~kSSFIndexMask);
+}
+
 // Cell product P_A at point p over the atoms in the chunk's distance order.
-// The atoms come four at a time: their distances and R_AB^-1 are loaded
-// together before the factors are applied in order, so that four loads are
-// in flight instead of one.
 __device__ __forceinline__ double cell_sorted(int A, int natoms, int64_t p, double h,
-                                              const uint64_t* __restrict__ keys,
+                                              const uint32_t* __restrict__ keys,
                                               const double* __restrict__ dist, int ld,
                                               const double* __restrict__ rab_inv, int ld_rab) {
-  constexpr int U = 4;
   const double rA = dist[(int64_t)A * ld + p];
   const double* rinv = rab_inv + (int64_t)A * ld_rab;
   // atoms with d_B >= lim have r_B >= kSSFFar r_A (1 + 1e-9): factor 1
   const double lim = kSSFFar * rA * (1. + 1e-9) + h;
   double ps = 1.;
-  for (int k = 0; k < natoms; k += U) {
-    int B[U];
-    bool use[U];
-    double rB[U], ri[U];
-    int nv = U;  // entries of this group before the first one at or beyond lim
-#pragma unroll
-    for (int j = 0; j < U; ++j) {
-      const int kk = k + j;
-      const uint64_t key = kk < natoms ? keys[kk] : ~0ull;
-      const bool in = kk < natoms && (double)__uint_as_float((unsigned)(key >> 32)) < lim;
-      if (!in && j < nv) nv = j;
-      B[j] = (int)(key & 0xFFFFu);
-      use[j] = in && j < nv && B[j] != A;
-      rB[j] = use[j] ? dist[(int64_t)B[j] * ld + p] : 0.;
-      ri[j] = use[j] ? rinv[B[j]] : 0.;
-    }
-#pragma unroll
-    for (int j = 0; j < U; ++j) {
-      if (j >= nv) return ps;
-      if (!use[j]) continue;
-      const double mu = (rA - rB[j]) * ri[j];
-      if (mu >= kSSFa) return 0.;
-      if (mu > -kSSFa) {
-        ps *= ssf_s(mu);
-        if (ps <= kSSFTol) return ps;
-      }
+  for (int k = 0; k < natoms; ++k) {
+    const uint32_t key = keys[k];
+    if (key_dist(key) >= lim) break;
+    const int B = (int)(key & kSSFIndexMask);
+    if (B == A) continue;
+    const double mu = (rA - dist[(int64_t)B * ld + p]) * rinv[B];
+    if (mu >= kSSFa) return 0.;
+    if (mu > -kSSFa) {
+      ps *= ssf_s(mu);
+      if (ps <= kSSFTol) break;
     }
   }
   return ps;
@@ -177,10 +166,10 @@ __global__ void __launch_bounds__(kSSFWarps * 32)
                         const double* __restrict__ coords, const double* __restrict__ rab_inv,
                         int ld_rab, const double* __restrict__ dist, int ld,
                         double* __restrict__ weights, int* __restrict__ status) {
-  extern __shared__ uint64_t ssf_smem[];
+  extern __shared__ uint32_t ssf_smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // per warp: nsort sort keys, then up to nsort candidate atoms (uint16)
-  uint64_t* keys = ssf_smem + (size_t)warp * (nsort + nsort / 4);
+  uint32_t* keys = ssf_smem + (size_t)warp * (nsort + nsort / 2);
   uint16_t* cand = reinterpret_cast<uint16_t*>(keys + nsort);
   const int64_t p0 = ((int64_t)blockIdx.x * kSSFWarps + warp) * 32;
   if (p0 >= npts) return;  // the whole warp
@@ -196,11 +185,11 @@ __global__ void __launch_bounds__(kSSFWarps * 32)
 
   // ---- atoms in distance order (keys: d_B as float rounded down, atom index)
   for (int b = lane; b < nsort; b += 32) {
-    uint64_t k = ~0ull;
+    uint32_t k = ~0u;
     if (b < natoms) {
       const double dx = cx - coords[3 * b], dy = cy - coords[3 * b + 1], dz = cz - coords[3 * b + 2];
       const float df = __double2float_rd(sqrt(dx * dx + dy * dy + dz * dz));
-      k = ((uint64_t)__float_as_uint(df) << 32) | (uint64_t)b;
+      k = (__float_as_uint(df) & ~kSSFIndexMask) | (uint32_t)b;
     }
     keys[b] = k;
   }
@@ -210,7 +199,7 @@ __global__ void __launch_bounds__(kSSFWarps * 32)
       for (int i = lane; i < nsort; i += 32) {
         const int ixj = i ^ j;
         if (ixj > i) {
-          const uint64_t u = keys[i], v = keys[ixj];
+          const uint32_t u = keys[i], v = keys[ixj];
           if ((u > v) == ((i & kk) == 0)) {
             keys[i] = v;
             keys[ixj] = u;
@@ -225,7 +214,7 @@ __global__ void __launch_bounds__(kSSFWarps * 32)
   double kd[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
-    kb[q] = q < natoms ? (int)(keys[q] & 0xFFFFu) : -1;
+    kb[q] = q < natoms ? (int)(keys[q] & kSSFIndexMask) : -1;
     if (kb[q] >= 0) {
       const double dx = cx - coords[3 * kb[q]], dy = cy - coords[3 * kb[q] + 1],
                    dz = cz - coords[3 * kb[q] + 2];
@@ -292,12 +281,13 @@ void launch_ssf_weights_screened(int64_t npts, int natoms, const double* x, cons
   grid_to_center_kernel<<<g1, threads, 0, s>>>(npts, natoms, x, y, z, coords, dist_scr, ld_dist);
   int nsort = 32;
   while (nsort < natoms) nsort <<= 1;
-  const size_t smem = (size_t)kSSFWarps * (nsort + nsort / 4) * sizeof(uint64_t);
+  const size_t smem = (size_t)kSSFWarps * (nsort + nsort / 2) * sizeof(uint32_t);
   static bool attr = false;
   if (!attr) {
-    GB300_CUDA(cudaFuncSetAttribute(ssf_screened_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)((size_t)kSSFWarps * (kSSFScreenedMaxAtoms + kSSFScreenedMaxAtoms / 4) *
-                                          sizeof(uint64_t))));
+    GB300_CUDA(cudaFuncSetAttribute(
+        ssf_screened_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        (int)((size_t)kSSFWarps * (kSSFScreenedMaxAtoms + kSSFScreenedMaxAtoms / 2) *
+              sizeof(uint32_t))));
     attr = true;
   }
   const int64_t chunks = (npts + 31) / 32;

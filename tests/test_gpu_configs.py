@@ -78,6 +78,9 @@ def test_workload_sample_matches_oracle(g, idx, ntasks, lwd):
                                   "Default").get_instance(g.functional_type(s["functional"]), lb)
     exc, vxc = integ.eval_exc_vxc(s["P"])
     tol = GATES[lwd]
+    print(f"\n[parity] workload {idx} ({lb.ntasks()} sampled tasks) {lwd}: |dEXC| "
+          f"{abs(exc - eo):.2e} max|dVXC| {np.abs(vxc - Vo).max():.2e} "
+          f"|dN_el| {abs(integ.last_nel() - no):.2e}")
     assert abs(exc - eo) <= tol, (exc, eo)
     assert np.abs(vxc - Vo).max() <= tol
     assert abs(integ.last_nel() - no) <= tol
@@ -117,6 +120,8 @@ def test_workload3_members_match_oracle(g):
         integs = [f.get_instance(g.functional_type(s["functional"]), lb) for s, lb in systems]
         for integ, (s, lb), (eo, Vo, no) in zip(integs, systems, refs):
             exc, vxc = integ.eval_exc_vxc(s["P"])
+            print(f"\n[parity] workload 3 member ({s['n_water']} waters, {s['functional']}) "
+                  f"{lwd}: |dEXC| {abs(exc - eo):.2e} max|dVXC| {np.abs(vxc - Vo).max():.2e}")
             assert abs(exc - eo) <= tol and np.abs(vxc - Vo).max() <= tol
             assert abs(integ.last_nel() - no) <= tol
         # the batched path: first call captures the graph, the second replays it

@@ -39,6 +39,8 @@ def test_mixed_matches_oracle(g, fname, func):
     exc, vxc = integ.eval_exc_vxc(d["P"])
     eo, Vo, no = oracle.eval_exc_vxc(oracle_basis(basis), oracle_ssf_tasks(tasks0, mol.coords()),
                                      d["P"], func)
+    print(f"\n[parity] benzene {func} mixed: |dEXC| {abs(exc - eo):.2e} "
+          f"max|dVXC| {np.abs(vxc - Vo).max():.2e}")
     assert abs(exc - eo) <= TOL_EXC
     assert np.abs(vxc - Vo).max() <= TOL_VXC
     assert abs(integ.last_nel() - no) <= 1e-8

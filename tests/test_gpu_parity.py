@@ -90,6 +90,9 @@ def test_exc_vxc_fp64_matches_oracle_and_golden(g, fname, func, prune):
     # oracle on the same task list with its own (host-algorithm) SSF weights
     eo, Vo, no = oracle.eval_exc_vxc(oracle_basis(basis), oracle_ssf_tasks(tasks0, mol.coords()),
                                      d["P"], func)
+    print(f"\n[parity] benzene {func} {prune} FP64: vs oracle |dEXC| {abs(exc - eo):.2e} "
+          f"max|dVXC| {np.abs(vxc - Vo).max():.2e}; vs golden |dEXC| {abs(exc - d['EXC'][0]):.2e} "
+          f"|dVXC|/nbf {np.linalg.norm(vxc - d['VXC']) / len(vxc):.2e}")
     assert abs(exc - eo) <= TOL_EXC
     assert np.abs(vxc - Vo).max() <= TOL_VXC
     assert abs(integ.last_nel() - no) <= 1e-10

@@ -43,6 +43,12 @@ def test_uks_svwn5_cytosine(g, lwd):
     integ = _integ(g, lb, "SVWN5", lwd)
     exc, Vs, Vz = integ.eval_exc_vxc_uks(d["Ps"], d["Pz"])
     tol = GATES[lwd]
+    nbf = len(Vs)
+    print(f"\n[parity] UKS cytosine SVWN5 {lwd}: vs oracle |dEXC| {abs(exc - eo):.2e} "
+          f"max|dVXC_s| {np.abs(Vs - Vso).max():.2e} max|dVXC_z| {np.abs(Vz - Vzo).max():.2e}; "
+          f"vs golden |dEXC| {abs(exc - d['EXC'][0]):.2e} "
+          f"|dVXC_s|/nbf {np.linalg.norm(Vs - d['VXCs']) / nbf:.2e} "
+          f"|dVXC_z|/nbf {np.linalg.norm(Vz - d['VXCz']) / nbf:.2e}")
     assert abs(exc - eo) <= tol
     assert np.abs(Vs - Vso).max() <= tol and np.abs(Vz - Vzo).max() <= tol
     assert abs(integ.last_nel() - no) <= tol
@@ -81,6 +87,8 @@ def test_uks_pbe_open_shell(g, lwd):
     s, lb, Ps, Pz, (eo, Vso, Vzo, no), _ = _waters(g)
     exc, Vs, Vz = _integ(g, lb, "PBE", lwd).eval_exc_vxc_uks(Ps, Pz)
     tol = GATES[lwd]
+    print(f"\n[parity] UKS 4 waters PBE open shell {lwd}: |dEXC| {abs(exc - eo):.2e} "
+          f"max|dVXC_s| {np.abs(Vs - Vso).max():.2e} max|dVXC_z| {np.abs(Vz - Vzo).max():.2e}")
     assert abs(exc - eo) <= tol
     assert np.abs(Vs - Vso).max() <= tol and np.abs(Vz - Vzo).max() <= tol
 
