@@ -26,6 +26,7 @@ __all__ = [
     "DeviceRuntimeEnvironment", "LoadBalancer", "LoadBalancerFactory",
     "MolecularWeightsSettings", "MolecularWeights", "MolecularWeightsFactory",
     "functional_type", "XCIntegrator", "XCIntegratorFactory", "IntegratorBatch", "lib",
+    "LocalDeviceWorkDriver", "XCDeviceData",
     "device_count",
     "ssf_weights", "collocation", "set_device", "measure_fp64_peak", "host_register",
     "host_unregister",
@@ -545,6 +546,79 @@ class XCIntegratorFactory:
         integ._lb = lb
         integ._func = func
         return integ
+
+
+# ------------------------------------------------------------------ stage-level work driver
+class XCDeviceData(_Handle):
+    """Device data of the stage-level work driver: tasks [begin, end) of a
+    weighted load balancer with every intermediate on the device."""
+    _delete = "gauxc_gb300_lwd_device_data_delete"
+
+
+class LocalDeviceWorkDriver:
+    """The reference's LocalDeviceWorkDriver stages
+    (src/xc_integrator/local_work_driver/device/local_device_work_driver.hpp:62-127),
+    FP64, one call per stage on an XCDeviceData."""
+
+    def create_device_data(self, lb, task_begin=0, task_end=None):
+        end = lb.ntasks() if task_end is None else task_end
+        d = XCDeviceData(_call(_L.gauxc_gb300_lwd_device_data_new, lb._h,
+                               ctypes.c_int64(task_begin), ctypes.c_int64(end)))
+        d._lb = lb
+        d._nbf = lb._keep[3].nbf()
+        return d
+
+    def eval_collocation(self, d):
+        _call(_L.gauxc_gb300_lwd_eval_collocation, d._h, ctypes.c_bool(False))
+
+    def eval_collocation_gradient(self, d):
+        _call(_L.gauxc_gb300_lwd_eval_collocation, d._h, ctypes.c_bool(True))
+
+    def eval_xmat(self, fac, d, P):
+        P = np.asfortranarray(P, dtype=np.float64)
+        _call(_L.gauxc_gb300_lwd_eval_xmat, d._h, ctypes.c_double(fac),
+              P.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.c_int64(P.shape[0]))
+
+    def eval_vvars_lda(self, d):
+        _call(_L.gauxc_gb300_lwd_eval_vvars, d._h, ctypes.c_bool(False))
+
+    def eval_vvars_gga(self, d):
+        _call(_L.gauxc_gb300_lwd_eval_vvars, d._h, ctypes.c_bool(True))
+
+    def eval_uvars_gga(self, d):
+        _call(_L.gauxc_gb300_lwd_eval_uvars, d._h)
+
+    def eval_kern_exc_vxc_lda(self, func, d):
+        _call(_L.gauxc_gb300_lwd_eval_kern_exc_vxc, d._h, func._h)
+
+    eval_kern_exc_vxc_gga = eval_kern_exc_vxc_lda
+
+    def inc_exc(self, d):
+        _call(_L.gauxc_gb300_lwd_inc_exc, d._h)
+
+    def inc_nel(self, d):
+        _call(_L.gauxc_gb300_lwd_inc_nel, d._h)
+
+    def eval_zmat_lda_vxc(self, d):
+        _call(_L.gauxc_gb300_lwd_eval_zmat_vxc, d._h, ctypes.c_bool(False))
+
+    def eval_zmat_gga_vxc(self, d):
+        _call(_L.gauxc_gb300_lwd_eval_zmat_vxc, d._h, ctypes.c_bool(True))
+
+    def inc_vxc(self, d):
+        _call(_L.gauxc_gb300_lwd_inc_vxc, d._h)
+
+    def symmetrize_vxc(self, d):
+        V = np.zeros((d._nbf, d._nbf), order="F")
+        _call(_L.gauxc_gb300_lwd_symmetrize_vxc, d._h,
+              V.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.c_int64(d._nbf))
+        return V
+
+    def results(self, d):
+        """(EXC, N_el) accumulated by inc_exc / inc_nel."""
+        e, n = ctypes.c_double(), ctypes.c_double()
+        _call(_L.gauxc_gb300_lwd_results, d._h, ctypes.byref(e), ctypes.byref(n))
+        return e.value, n.value
 
 
 # ------------------------------------------------------------------ stage entry points

@@ -32,6 +32,7 @@ GauXCMolecularWeightsFactory = _handle("GauXCMolecularWeightsFactory")
 GauXCFunctional = _handle("GauXCFunctional")
 GauXCIntegrator = _handle("GauXCIntegrator")
 GauXCGB300Batch = _handle("GauXCGB300Batch")
+GauXCGB300DeviceData = _handle("GauXCGB300DeviceData")
 
 
 class GauXCAtom(ctypes.Structure):
@@ -101,6 +102,19 @@ PROTOTYPES = {
                                              i64, P(dbl)]),
     "gauxc_integrator_eval_exc_vxc_uks": (None, [S, GauXCIntegrator, i64, i64, P(dbl), i64,
                                                  P(dbl), i64, P(dbl), P(dbl), i64, P(dbl), i64]),
+    "gauxc_gb300_lwd_device_data_new": (GauXCGB300DeviceData, [S, GauXCLoadBalancer, i64, i64]),
+    "gauxc_gb300_lwd_device_data_delete": (None, [S, P(GauXCGB300DeviceData)]),
+    "gauxc_gb300_lwd_eval_collocation": (None, [S, GauXCGB300DeviceData, b]),
+    "gauxc_gb300_lwd_eval_xmat": (None, [S, GauXCGB300DeviceData, dbl, P(dbl), i64]),
+    "gauxc_gb300_lwd_eval_vvars": (None, [S, GauXCGB300DeviceData, b]),
+    "gauxc_gb300_lwd_eval_uvars": (None, [S, GauXCGB300DeviceData]),
+    "gauxc_gb300_lwd_eval_kern_exc_vxc": (None, [S, GauXCGB300DeviceData, GauXCFunctional]),
+    "gauxc_gb300_lwd_inc_exc": (None, [S, GauXCGB300DeviceData]),
+    "gauxc_gb300_lwd_inc_nel": (None, [S, GauXCGB300DeviceData]),
+    "gauxc_gb300_lwd_eval_zmat_vxc": (None, [S, GauXCGB300DeviceData, b]),
+    "gauxc_gb300_lwd_inc_vxc": (None, [S, GauXCGB300DeviceData]),
+    "gauxc_gb300_lwd_symmetrize_vxc": (None, [S, GauXCGB300DeviceData, P(dbl), i64]),
+    "gauxc_gb300_lwd_results": (None, [S, GauXCGB300DeviceData, P(dbl), P(dbl)]),
     "gauxc_gb300_version": (ctypes.c_char_p, []),
     "gauxc_gb300_device_count": (I, []),
     "gauxc_gb300_basisset_nshells": (sz, [S, GauXCBasisSet]),

@@ -136,6 +136,9 @@ void gauxc_object_delete(GauXCStatus* status, void** handle) {
     case GauXC_Type_Functional: gauxc_functional_delete(status, (GauXCFunctional*)*handle); break;
     case GauXC_Type_Integrator: gauxc_integrator_delete(status, (GauXCIntegrator*)*handle); break;
     case GauXC_Type_GB300Batch: gauxc_gb300_batch_delete(status, (GauXCGB300Batch*)*handle); break;
+    case GauXC_Type_GB300DeviceData:
+      gauxc_gb300_lwd_device_data_delete(status, (GauXCGB300DeviceData*)*handle);
+      break;
     default: status_fail(status, "unknown handle type");
   }
 }
@@ -951,6 +954,82 @@ void gauxc_gb300_collocation(GauXCStatus* status, const GauXCBasisSet basis, int
   guarded(status, [&] {
     collocation_device(*b, npts, points, nshells, shell_list, grad, phi, dphi_x, dphi_y, dphi_z);
   });
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- stage-level work driver
+namespace {
+template <typename F>
+void lwd_call(GauXCStatus* status, const GauXCGB300DeviceData& d, F&& f) {
+  status_init(status);
+  if (!check(status, d, GauXC_Type_GB300DeviceData, "DeviceData")) return;
+  guarded(status, [&] { f(*deref<LWDData>(d.ptr)); });
+}
+}  // namespace
+
+extern "C" {
+
+GauXCGB300DeviceData gauxc_gb300_lwd_device_data_new(GauXCStatus* status,
+                                                     const GauXCLoadBalancer lb,
+                                                     int64_t task_begin, int64_t task_end) {
+  status_init(status);
+  GauXCGB300DeviceData h{};
+  h.hdr.type = GauXC_Type_GB300DeviceData;
+  if (!check(status, lb, GauXC_Type_LoadBalancer, "LoadBalancer")) return h;
+  guarded(status, [&] {
+    h = make_handle<GauXCGB300DeviceData>(
+        GauXC_Type_GB300DeviceData, lwd_create(*deref<LoadBalancer>(lb.ptr), task_begin, task_end));
+  });
+  return h;
+}
+
+void gauxc_gb300_lwd_device_data_delete(GauXCStatus* status, GauXCGB300DeviceData* data) {
+  status_init(status);
+  destroy<LWDData>(data);
+}
+
+void gauxc_gb300_lwd_eval_collocation(GauXCStatus* status, const GauXCGB300DeviceData data,
+                                      bool gradient) {
+  lwd_call(status, data, [&](LWDData& d) { lwd_eval_collocation(d, gradient); });
+}
+void gauxc_gb300_lwd_eval_xmat(GauXCStatus* status, const GauXCGB300DeviceData data, double fac,
+                               const double* P, int64_t ldp) {
+  lwd_call(status, data, [&](LWDData& d) { lwd_eval_xmat(d, fac, P, ldp); });
+}
+void gauxc_gb300_lwd_eval_vvars(GauXCStatus* status, const GauXCGB300DeviceData data, bool gga) {
+  lwd_call(status, data, [&](LWDData& d) { lwd_eval_vvars(d, gga); });
+}
+void gauxc_gb300_lwd_eval_uvars(GauXCStatus* status, const GauXCGB300DeviceData data) {
+  lwd_call(status, data, [&](LWDData& d) { lwd_eval_uvars(d); });
+}
+void gauxc_gb300_lwd_eval_kern_exc_vxc(GauXCStatus* status, const GauXCGB300DeviceData data,
+                                       const GauXCFunctional functional) {
+  status_init(status);
+  if (!check(status, functional, GauXC_Type_Functional, "Functional")) return;
+  lwd_call(status, data, [&](LWDData& d) {
+    lwd_eval_kern_exc_vxc(d, *deref<XCFunctionalDesc>(functional.ptr));
+  });
+}
+void gauxc_gb300_lwd_inc_exc(GauXCStatus* status, const GauXCGB300DeviceData data) {
+  lwd_call(status, data, [&](LWDData& d) { lwd_inc_exc(d); });
+}
+void gauxc_gb300_lwd_inc_nel(GauXCStatus* status, const GauXCGB300DeviceData data) {
+  lwd_call(status, data, [&](LWDData& d) { lwd_inc_nel(d); });
+}
+void gauxc_gb300_lwd_eval_zmat_vxc(GauXCStatus* status, const GauXCGB300DeviceData data, bool gga) {
+  lwd_call(status, data, [&](LWDData& d) { lwd_eval_zmat_vxc(d, gga); });
+}
+void gauxc_gb300_lwd_inc_vxc(GauXCStatus* status, const GauXCGB300DeviceData data) {
+  lwd_call(status, data, [&](LWDData& d) { lwd_inc_vxc(d); });
+}
+void gauxc_gb300_lwd_symmetrize_vxc(GauXCStatus* status, const GauXCGB300DeviceData data,
+                                    double* vxc, int64_t ldvxc) {
+  lwd_call(status, data, [&](LWDData& d) { lwd_symmetrize_vxc(d, vxc, ldvxc); });
+}
+void gauxc_gb300_lwd_results(GauXCStatus* status, const GauXCGB300DeviceData data, double* exc,
+                             double* nel) {
+  lwd_call(status, data, [&](LWDData& d) { lwd_results(d, exc, nel); });
 }
 
 }  // extern "C"

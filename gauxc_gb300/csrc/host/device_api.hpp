@@ -116,6 +116,22 @@ void set_device(int dev);
 void screen_boxes_device(const std::vector<double>& boxes, const BasisSet& bs,
                          std::vector<uint32_t>& bits, int& nwords);
 
+// Stage-level local work driver (lwd.cu): one device-data object over tasks
+// [t0, t1) of a weighted load balancer, and the reference's stages on it.
+class LWDData;
+std::shared_ptr<LWDData> lwd_create(const LoadBalancer& lb, int64_t t0, int64_t t1);
+void lwd_eval_collocation(LWDData& d, bool grad);
+void lwd_eval_xmat(LWDData& d, double fac, const double* P, int64_t ldp);
+void lwd_eval_vvars(LWDData& d, bool gga);
+void lwd_eval_uvars(LWDData& d);
+void lwd_eval_kern_exc_vxc(LWDData& d, const XCFunctionalDesc& f);
+void lwd_inc_exc(LWDData& d);
+void lwd_inc_nel(LWDData& d);
+void lwd_eval_zmat_vxc(LWDData& d, bool gga);
+void lwd_inc_vxc(LWDData& d);
+void lwd_symmetrize_vxc(LWDData& d, double* VXC, int64_t ld);
+void lwd_results(LWDData& d, double* exc, double* nel);
+
 // SSF weights on the device for every task of the load balancer.
 void molecular_weights_ssf_device(LoadBalancer& lb, RuntimeEnv& rt);
 

@@ -52,7 +52,9 @@ enum GauXC_Type {
   GauXC_Type_Functional = 9,
   GauXC_Type_Integrator = 10,
   /* extension: handle of a batch of integrators (gauxc_gb300_batch_new) */
-  GauXC_Type_GB300Batch = 64
+  GauXC_Type_GB300Batch = 64,
+  /* extension: device data of the stage-level work driver (gauxc_gb300_lwd_*) */
+  GauXC_Type_GB300DeviceData = 65
 };
 
 /* include/gauxc/c/types.h:42 */
@@ -129,6 +131,8 @@ typedef struct GauXCFunctional { GauXCHeader hdr; void* ptr; } GauXCFunctional;
 typedef struct GauXCIntegrator { GauXCHeader hdr; void* ptr; } GauXCIntegrator;
 /* extension: many integrators evaluated by one CUDA-graph launch */
 typedef struct GauXCGB300Batch { GauXCHeader hdr; void* ptr; } GauXCGB300Batch;
+/* extension: device data of the stage-level work driver */
+typedef struct GauXCGB300DeviceData { GauXCHeader hdr; void* ptr; } GauXCGB300DeviceData;
 
 /* include/gauxc/c/molecular_weights.h:34 */
 typedef struct GauXCMolecularWeightsSettings {
@@ -390,6 +394,41 @@ void gauxc_gb300_batch_eval_exc_vxc_rks(GauXCStatus* status, const GauXCGB300Bat
 int gauxc_gb300_batch_timings(GauXCStatus* status, const GauXCGB300Batch batch, double* out,
                               int nmax);
 void gauxc_gb300_batch_delete(GauXCStatus* status, GauXCGB300Batch* batch);
+
+/* ---- stage-level local work driver
+   The stages of the reference's LocalDeviceWorkDriver
+   (src/xc_integrator/local_work_driver/device/local_device_work_driver.hpp:62-127)
+   on a device-data object (XCDeviceData, xc_device_data.hpp:668-787) that holds
+   tasks [task_begin, task_end) of a load balancer with modified weights, all
+   in FP64 with every intermediate kept on the device.  One SCF evaluation, in
+   the reference integrator's order
+   (incore_replicated_xc_device_integrator_exc_vxc.hpp:283-404):
+     eval_collocation (gradient for GGA), eval_xmat (fac = 2 for an RKS alpha
+     density), eval_vvars (gga), eval_uvars (GGA), eval_kern_exc_vxc, inc_exc,
+     inc_nel, eval_zmat_vxc (gga), inc_vxc, symmetrize_vxc, results.
+   EXC, N_el and VXC accumulate over the calls until the object is deleted. */
+GauXCGB300DeviceData gauxc_gb300_lwd_device_data_new(GauXCStatus* status,
+                                                     const GauXCLoadBalancer lb,
+                                                     int64_t task_begin, int64_t task_end);
+void gauxc_gb300_lwd_device_data_delete(GauXCStatus* status, GauXCGB300DeviceData* data);
+void gauxc_gb300_lwd_eval_collocation(GauXCStatus* status, const GauXCGB300DeviceData data,
+                                      bool gradient);
+/* X = fac * P_sub * phi, P column-major nbf x nbf (host, leading dimension ldp) */
+void gauxc_gb300_lwd_eval_xmat(GauXCStatus* status, const GauXCGB300DeviceData data, double fac,
+                               const double* P, int64_t ldp);
+void gauxc_gb300_lwd_eval_vvars(GauXCStatus* status, const GauXCGB300DeviceData data, bool gga);
+void gauxc_gb300_lwd_eval_uvars(GauXCStatus* status, const GauXCGB300DeviceData data);
+void gauxc_gb300_lwd_eval_kern_exc_vxc(GauXCStatus* status, const GauXCGB300DeviceData data,
+                                       const GauXCFunctional functional);
+void gauxc_gb300_lwd_inc_exc(GauXCStatus* status, const GauXCGB300DeviceData data);
+void gauxc_gb300_lwd_inc_nel(GauXCStatus* status, const GauXCGB300DeviceData data);
+void gauxc_gb300_lwd_eval_zmat_vxc(GauXCStatus* status, const GauXCGB300DeviceData data, bool gga);
+void gauxc_gb300_lwd_inc_vxc(GauXCStatus* status, const GauXCGB300DeviceData data);
+/* VXC = A + A^T of the accumulated contributions into vxc (host, leading dimension ldvxc) */
+void gauxc_gb300_lwd_symmetrize_vxc(GauXCStatus* status, const GauXCGB300DeviceData data,
+                                    double* vxc, int64_t ldvxc);
+void gauxc_gb300_lwd_results(GauXCStatus* status, const GauXCGB300DeviceData data, double* exc,
+                             double* nel);
 
 #ifdef __cplusplus
 }

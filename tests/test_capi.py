@@ -99,6 +99,8 @@ def test_device_paths_fail_loudly_without_gpu(g):
         mw.modify_weights(lb)
     with pytest.raises(GauXCError, match="no CUDA device"):
         _tiny_system(g, g.ExecutionSpace.Device)  # the Device load balancer screens on the GPU
+    with pytest.raises(GauXCError, match="Weights Have Not Been Modified|no CUDA device"):
+        g.LocalDeviceWorkDriver().create_device_data(lb)
     with pytest.raises(GauXCError, match="no CUDA device"):
         g.collocation(basis, np.zeros((4, 3)), [0, 1])
 
