@@ -159,8 +159,13 @@ class DeviceIntegrator {
   int64_t enqueue_uks(const double* Ps, int64_t ldps, const double* Pz, int64_t ldpz,
                       double* VXCs, int64_t ldvs, double* VXCz, int64_t ldvz, double* en_host,
                       int* err_host, bool do_vxc);
-  // brings a caller density matrix in as c P (c a power of two)
-  int64_t load_density(const double* P, int64_t ldp, double* dst, double c);
+  // brings a caller density matrix in as c P (c a power of two), in the
+  // device AO order; `stage` (n x n) receives the caller's matrix first when
+  // that order is a permutation
+  int64_t load_density(const double* P, int64_t ldp, double* dst, double c, double* stage);
+  // VXC = A + A^T, in the caller's AO order, into V (device or host memory the
+  // device addresses)
+  void symmetrize_out(const double* A, double* V, int64_t ld);
   // VXC = A + A^T out to the caller (host_direct_: straight; otherwise staged)
   int64_t store_vxc(const double* A, double* stage, double* VXC, int64_t ldvxc);
   void ensure_uks();
@@ -190,6 +195,10 @@ class DeviceIntegrator {
   double* A_ = nullptr;
   double* V_ = nullptr;
   double* out_ = nullptr;
+  // mixed path: P_ and A_ are held in a permuted AO order (perm_: position ->
+  // caller's AO index, iperm_ its inverse); null on the FP64 path
+  int* perm_ = nullptr;
+  int* iperm_ = nullptr;
   int64_t npts_plan_ = 0;
   // UKS work space (first polarized call): the z density, its VXC
   // accumulator (and staging), (rho, grad rho) of both densities, Z_z
@@ -521,6 +530,58 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
   std::vector<int> order(pbs.size());
   std::iota(order.begin(), order.end(), 0);
 
+  // Device AO order.  A block's union basis holds, for every cutoff radius,
+  // the shells of that radius whose centres lie within reach of its points:
+  // in the caller's order (atom by atom) that is a patchwork of short shell
+  // runs.  Here the shells are ordered by cutoff radius (largest first), then
+  // by the Morton code of their centre, so a block's union becomes a few long
+  // runs per radius, and the P gather and the VXC atomics touch fewer DRAM
+  // sectors.  P_ and A_ live in this order; P comes in and VXC goes out
+  // through permuting copies.
+  const int nsh_all = (int)bs.shells.size();
+  std::vector<int> shell_pos(nsh_all), new_off(nsh_all);
+  {
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (const auto& sh : bs.shells)
+      for (int k = 0; k < 3; ++k) {
+        lo[k] = std::min(lo[k], sh.O[k]);
+        hi[k] = std::max(hi[k], sh.O[k]);
+      }
+    auto morton = [&](const double* O) {
+      uint64_t code = 0;
+      for (int k = 0; k < 3; ++k) {
+        const double span = hi[k] - lo[k];
+        const uint64_t q = span > 0. ? (uint64_t)std::min(1023., (O[k] - lo[k]) / span * 1023.) : 0;
+        for (int bit = 0; bit < 10; ++bit) code |= ((q >> bit) & 1ull) << (3 * bit + k);
+      }
+      return code;
+    };
+    std::vector<uint64_t> mc(nsh_all);
+    for (int x = 0; x < nsh_all; ++x) mc[x] = morton(bs.shells[x].O);
+    std::vector<int> ord(nsh_all);
+    std::iota(ord.begin(), ord.end(), 0);
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
+      const Shell &sa = bs.shells[a], &sb = bs.shells[b];
+      if (sa.cutoff_radius != sb.cutoff_radius) return sa.cutoff_radius > sb.cutoff_radius;
+      if (sa.l != sb.l) return sa.l < sb.l;
+      return mc[a] < mc[b];
+    });
+    std::vector<int> perm(nbf_), iperm(nbf_);
+    int o = 0;
+    for (int k = 0; k < nsh_all; ++k) {
+      const int x = ord[k];
+      shell_pos[x] = k;
+      new_off[x] = o;
+      for (int f = 0; f < bs.shells[x].size(); ++f) {
+        perm[o + f] = bs.shell_offs[x] + f;
+        iperm[bs.shell_offs[x] + f] = o + f;
+      }
+      o += bs.shells[x].size();
+    }
+    perm_ = arena_.upload(perm, s);
+    iperm_ = arena_.upload(iperm, s);
+  }
+
   const int npb = (int)pbs.size();
   std::vector<int64_t> pt_off(npb), bf_off(npb), sh_off(npb), f64_off(npb), dig_off(npb),
       mask_off(npb);
@@ -540,18 +601,23 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
     nsh[i] = (int)b.shells.size();
     sh_off[i] = (int64_t)sh_list.size();
     bf_off[i] = (int64_t)bf_list.size();
+    // the union's columns in device AO order (shell data stays indexed by
+    // the caller's shell index)
+    std::vector<int> ushells(b.shells);
+    std::sort(ushells.begin(), ushells.end(),
+              [&](int a, int c) { return shell_pos[a] < shell_pos[c]; });
     int col = 0;
-    for (int x : b.shells) {
+    for (int x : ushells) {
       sh_list.push_back(x);
       sh_col.push_back(col);
-      for (int k = 0; k < bs.shells[x].size(); ++k) bf_list.push_back(bs.shell_offs[x] + k);
+      for (int k = 0; k < bs.shells[x].size(); ++k) bf_list.push_back(new_off[x] + k);
       col += bs.shells[x].size();
     }
     for (int k = col; k < nu_pad[i]; ++k) bf_list.push_back(-1);
     mask_off[i] = (int64_t)mask.size();
     for (size_t m = 0; m < b.segs.size(); ++m) {
       const XCTask& tt = tasks[b.segs[m].task];
-      for (int x : b.shells)
+      for (int x : ushells)
         mask.push_back(std::binary_search(tt.shell_list.begin(), tt.shell_list.end(), x) ? 1 : 0);
     }
     int np_real = 0;
@@ -605,7 +671,7 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
   size_t free_b = 0, total_b = 0;
   GB300_CUDA(cudaMemGetInfo(&free_b, &total_b));
   double static_bytes = pts * (3 * 8. + 8. + 32. + 32. + 4.) + bf_list.size() * 4. +
-                        mask.size() + 64e6;
+                        mask.size() + 8. * nbf_ + 64e6;
   if (func_.polarized)  // ensure_uks
     static_bytes += 3. * nbf_ * nbf_ * 8. + pts * (32. + 32.) + nbf_ * 8.;
   double budget = rt_->user_mem ? (double)rt_->user_bytes - rt_->user_used - static_bytes
@@ -791,17 +857,9 @@ int64_t DeviceIntegrator::enqueue(const double* P, int64_t ldp, double* VXC, int
   // the error flag of this call's pipeline waits starts clear
   GB300_CUDA(cudaMemsetAsync(err_, 0, sizeof(int), s));
   if (events) GB300_CUDA(cudaEventRecord(ev_[0], s));
-  if (host_direct_) {
-    // the device reads the caller's (pageable or page-locked) P itself
-    launch_copy_matrix(P, ldp, P_, nbf_, nbf_, s);
-  } else if (ldp == nbf_) {
-    GB300_CUDA(cudaMemcpyAsync(P_, P, row * nbf_, cudaMemcpyHostToDevice, s));
-  } else {
-    GB300_CUDA(cudaMemcpy2DAsync(P_, row, P, (size_t)ldp * sizeof(double), row, nbf_,
-                                 cudaMemcpyHostToDevice, s));
-  }
+  // A_ (cleared next) stages the caller's P when the device order differs
+  int64_t launches = load_density(P, ldp, P_, 1., A_);
   if (events) GB300_CUDA(cudaEventRecord(ev_[1], s));
-  int64_t launches = host_direct_ ? 1 : 0;
   if (do_vxc) GB300_CUDA(cudaMemsetAsync(A_, 0, (size_t)nbf_ * nbf_ * sizeof(double), s));
   pev_used_ = 0;
   if (prec_ == Precision::Mixed) launches += eval_mixed_batches(do_vxc);
@@ -831,7 +889,7 @@ int64_t DeviceIntegrator::enqueue(const double* P, int64_t ldp, double* VXC, int
   }
   if (do_vxc && !host_direct_)
     launches += timed(4, [&] {
-      launch_symmetrize(A_, nbf_, V_, nbf_, s);
+      symmetrize_out(A_, V_, nbf_);
       return (int64_t)1;
     });
   launches += timed(4, [&] {
@@ -842,7 +900,7 @@ int64_t DeviceIntegrator::enqueue(const double* P, int64_t ldp, double* VXC, int
   if (do_vxc) {
     if (host_direct_) {
       // VXC = A + A^T written straight into the caller's buffer
-      launch_symmetrize(A_, nbf_, VXC, ldvxc, s);
+      symmetrize_out(A_, VXC, ldvxc);
       ++launches;
     } else if (ldvxc == nbf_) {
       GB300_CUDA(cudaMemcpyAsync(VXC, V_, row * nbf_, cudaMemcpyDeviceToHost, s));
@@ -858,34 +916,48 @@ int64_t DeviceIntegrator::enqueue(const double* P, int64_t ldp, double* VXC, int
   return launches;
 }
 
-int64_t DeviceIntegrator::load_density(const double* P, int64_t ldp, double* dst, double c) {
+int64_t DeviceIntegrator::load_density(const double* P, int64_t ldp, double* dst, double c,
+                                       double* stage) {
   cudaStream_t s = stream_;
   const size_t row = (size_t)nbf_ * sizeof(double);
+  // the caller's matrix lands coalesced (in `stage` when it is permuted next)
+  double* land = perm_ ? stage : dst;
   int64_t n = 0;
   if (host_direct_) {
-    launch_copy_matrix(P, ldp, dst, nbf_, nbf_, s);
+    // the device reads the caller's (pageable or page-locked) P itself
+    launch_copy_matrix(P, ldp, land, nbf_, nbf_, s);
     ++n;
   } else if (ldp == nbf_) {
-    GB300_CUDA(cudaMemcpyAsync(dst, P, row * nbf_, cudaMemcpyHostToDevice, s));
+    GB300_CUDA(cudaMemcpyAsync(land, P, row * nbf_, cudaMemcpyHostToDevice, s));
   } else {
-    GB300_CUDA(cudaMemcpy2DAsync(dst, row, P, (size_t)ldp * sizeof(double), row, nbf_,
+    GB300_CUDA(cudaMemcpy2DAsync(land, row, P, (size_t)ldp * sizeof(double), row, nbf_,
                                  cudaMemcpyHostToDevice, s));
   }
-  if (c != 1.) {
+  if (perm_) {
+    launch_permute_matrix(land, nbf_, perm_, c, dst, s);
+    ++n;
+  } else if (c != 1.) {
     launch_scale(dst, (int64_t)nbf_ * nbf_, c, s);
     ++n;
   }
   return n;
 }
 
+void DeviceIntegrator::symmetrize_out(const double* A, double* V, int64_t ld) {
+  if (iperm_)
+    launch_symmetrize_perm(A, nbf_, iperm_, V, ld, stream_);
+  else
+    launch_symmetrize(A, nbf_, V, ld, stream_);
+}
+
 int64_t DeviceIntegrator::store_vxc(const double* A, double* stage, double* VXC, int64_t ldvxc) {
   cudaStream_t s = stream_;
   const size_t row = (size_t)nbf_ * sizeof(double);
   if (host_direct_) {
-    launch_symmetrize(A, nbf_, VXC, ldvxc, s);
+    symmetrize_out(A, VXC, ldvxc);
     return 1;
   }
-  launch_symmetrize(A, nbf_, stage, nbf_, s);
+  symmetrize_out(A, stage, nbf_);
   if (ldvxc == nbf_)
     GB300_CUDA(cudaMemcpyAsync(VXC, stage, row * nbf_, cudaMemcpyDeviceToHost, s));
   else
@@ -958,7 +1030,9 @@ int64_t DeviceIntegrator::enqueue_uks(const double* Ps, int64_t ldps, const doub
   GB300_CUDA(cudaMemsetAsync(err_, 0, sizeof(int), s));
   GB300_CUDA(cudaEventRecord(ev_[0], s));
   // P_s / 2 and P_z / 2: the RKS passes (X = 2 P phi) then give X = P phi
-  int64_t launches = load_density(Ps, ldps, P_, 0.5) + load_density(Pz, ldpz, Pz_, 0.5);
+  // A_ and Az_ (cleared next) stage the caller's matrices when the device
+  // order differs
+  int64_t launches = load_density(Ps, ldps, P_, 0.5, A_) + load_density(Pz, ldpz, Pz_, 0.5, Az_);
   GB300_CUDA(cudaEventRecord(ev_[1], s));
   if (do_vxc) {
     GB300_CUDA(cudaMemsetAsync(A_, 0, (size_t)nbf_ * nbf_ * sizeof(double), s));

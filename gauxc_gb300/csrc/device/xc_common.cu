@@ -6,6 +6,8 @@
 // sums EXC / N_el with cublasDdot per batch (kernels/cublas_extensions.cu:
 // 86-112, plain FP64); this build reduces per-CTA partials in a fixed order
 // with Neumaier compensation, so the result is bit-reproducible.
+#include <algorithm>
+
 #include "xc_kernels.cuh"
 
 namespace gb300 {
@@ -29,6 +31,45 @@ __global__ void symmetrize_kernel(const double* __restrict__ A, int n, double* _
     const int row = r0 + tx, col = c0 + y;
     if (row < n && col < n)
       V[(int64_t)col * ld + row] = A[(int64_t)col * n + row] + T[tx][y];
+  }
+}
+
+// VXC(r, c) = A(ip[r], ip[c]) + A(ip[c], ip[r]): the accumulator A is held in
+// a permuted AO order (ip: caller's AO index -> position in A), VXC comes out
+// in the caller's order.  Both reads gather within one column of A; the
+// writes are coalesced along r.
+__global__ void symmetrize_perm_kernel(const double* __restrict__ A, int n,
+                                       const int* __restrict__ ip, double* __restrict__ V,
+                                       int64_t ld) {
+  __shared__ double T[32][33];
+  const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+  const int tx = threadIdx.x;
+  const int pr = r0 + tx < n ? ip[r0 + tx] : 0;
+  const int pc = c0 + tx < n ? ip[c0 + tx] : 0;
+  // T[y][x] = A(ip[c0 + x], ip[r0 + y])
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const int prow = __shfl_sync(0xffffffffu, pr, y);
+    if (r0 + y < n && c0 + tx < n) T[y][tx] = A[(int64_t)prow * n + pc];
+  }
+  __syncthreads();
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const int col = c0 + y;
+    const int pcol = __shfl_sync(0xffffffffu, pc, y);
+    if (r0 + tx < n && col < n) V[(int64_t)col * ld + r0 + tx] = A[(int64_t)pcol * n + pr] + T[tx][y];
+  }
+}
+
+// dst(r, c) = scale src(perm[r], perm[c]) for n x n matrices (leading
+// dimension n): the symmetric AO permutation (perm: position -> caller's AO
+// index).  A CTA row walks columns; its threads gather within one column.
+__global__ void permute_matrix_kernel(const double* __restrict__ src, int n,
+                                      const int* __restrict__ perm, double scale,
+                                      double* __restrict__ dst) {
+  for (int c = blockIdx.y; c < n; c += gridDim.y) {
+    const double* sc = src + (int64_t)perm[c] * n;
+    double* dc = dst + (int64_t)c * n;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
+      dc[r] = scale * sc[perm[r]];
   }
 }
 
@@ -70,6 +111,23 @@ __global__ void reduce_partials_kernel(const double2* __restrict__ p, int64_t n,
 void launch_symmetrize(const double* A, int nbf, double* vxc, int64_t ld, cudaStream_t s) {
   dim3 g((nbf + 31) / 32, (nbf + 31) / 32), b(32, 8);
   symmetrize_kernel<<<g, b, 0, s>>>(A, nbf, vxc, ld);
+  GB300_CUDA(cudaGetLastError());
+}
+
+void launch_symmetrize_perm(const double* A, int nbf, const int* iperm, double* vxc, int64_t ld,
+                            cudaStream_t s) {
+  if (nbf <= 0) return;
+  dim3 g((nbf + 31) / 32, (nbf + 31) / 32), b(32, 8);
+  symmetrize_perm_kernel<<<g, b, 0, s>>>(A, nbf, iperm, vxc, ld);
+  GB300_CUDA(cudaGetLastError());
+}
+
+void launch_permute_matrix(const double* src, int nbf, const int* perm, double scale, double* dst,
+                           cudaStream_t s) {
+  if (nbf <= 0) return;
+  const int gx = std::min((nbf + 255) / 256, 16);
+  dim3 g(gx, std::min(nbf, std::max(1, 4864 / gx)));
+  permute_matrix_kernel<<<g, 256, 0, s>>>(src, nbf, perm, scale, dst);
   GB300_CUDA(cudaGetLastError());
 }
 

@@ -30,6 +30,13 @@ void launch_vxc_fp64(const TasksDev& tk, const int4* items, int nitems, const do
 
 // VXC(i,j) = A(i,j) + A(j,i), written with leading dimension ld.
 void launch_symmetrize(const double* A, int nbf, double* vxc, int64_t ld, cudaStream_t s);
+// VXC = A + A^T in the caller's AO order from an accumulator held in a
+// permuted order (iperm: caller's AO index -> position in A)
+void launch_symmetrize_perm(const double* A, int nbf, const int* iperm, double* vxc, int64_t ld,
+                            cudaStream_t s);
+// dst = scale P(perm, perm) (perm: position -> caller's AO index), n x n, ld n
+void launch_permute_matrix(const double* src, int nbf, const int* perm, double scale, double* dst,
+                           cudaStream_t s);
 // dst = src for n x n column-major matrices; either may be device-addressable host memory.
 void launch_copy_matrix(const double* src, int64_t lds, double* dst, int64_t ldd, int n,
                         cudaStream_t s);
