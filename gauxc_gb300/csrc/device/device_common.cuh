@@ -69,14 +69,16 @@ void launch_ssf_weights(int64_t npts, int natoms, const double* x, const double*
                         cudaStream_t s);
 
 // The same weights with the cell products screened per chunk of 32 points
-// (ssf.cu); molecules of more than kSSFScreenedMaxAtoms atoms run the
-// reference-order kernel above.
+// and every factor classified in FP32 first (ssf.cu); natoms <=
+// kSSFScreenedMaxAtoms.  coords_f: (x - o, y - o, z - o, 0) of every atom in
+// FP32 for the origin o; margin: a bound on the FP32 error of mu (ssf.cu).
 constexpr int kSSFScreenedMaxAtoms = 2048;
 void launch_ssf_weights_screened(int64_t npts, int natoms, const double* x, const double* y,
                                  const double* z, const int32_t* iparent,
                                  const double* dist_nearest, const double* coords,
-                                 const double* rab_inv, int ld_rab, double* dist_scr, int ld_dist,
-                                 double* weights, int* status, cudaStream_t s);
+                                 const float4* coords_f, double ox, double oy, double oz,
+                                 float margin, const double* rab_inv, int ld_rab, double* weights,
+                                 int* status, cudaStream_t s);
 
 void launch_collocation(const ShellsDev& sh, const TasksDev& tk, const int2* items, int nitems,
                         double* scr, bool grad, cudaStream_t s);

@@ -12,7 +12,9 @@
 // 1e-13 or below; a parent product below machine epsilon zeroes the weight.
 //
 // Layout: distances are stored atom-major (dist[a * ld + p]) so that the
-// per-point loops read consecutive addresses across a warp.
+// per-point loops read consecutive addresses across a warp.  Every point-atom
+// distance, in the table or computed on the fly, is the same FP64 expression
+// (dist64), so the two kernels below see identical distances.
 #include "device_common.cuh"
 
 #include <algorithm>
@@ -24,6 +26,14 @@ namespace {
 constexpr double kSSFa = 0.64;
 constexpr double kSSFTol = 1e-13;
 
+// |p - c| in FP64 with every rounding spelled out (no contraction choices
+// left to the compiler): sqrt(fma(dz, dz, fma(dy, dy, dx * dx))).
+__device__ __forceinline__ double dist64(double px, double py, double pz,
+                                         const double* __restrict__ c) {
+  const double dx = __dsub_rn(px, c[0]), dy = __dsub_rn(py, c[1]), dz = __dsub_rn(pz, c[2]);
+  return __dsqrt_rn(__fma_rn(dz, dz, __fma_rn(dy, dy, __dmul_rn(dx, dx))));
+}
+
 __global__ void grid_to_center_kernel(int64_t npts, int natoms, const double* __restrict__ x,
                                       const double* __restrict__ y, const double* __restrict__ z,
                                       const double* __restrict__ coords, double* __restrict__ dist,
@@ -31,12 +41,8 @@ __global__ void grid_to_center_kernel(int64_t npts, int natoms, const double* __
   const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (p >= npts) return;
   const double px = x[p], py = y[p], pz = z[p];
-  for (int a = blockIdx.y; a < natoms; a += gridDim.y) {
-    const double dx = px - coords[3 * a + 0];
-    const double dy = py - coords[3 * a + 1];
-    const double dz = pz - coords[3 * a + 2];
-    dist[(int64_t)a * ld + p] = sqrt(dx * dx + dy * dy + dz * dz);
-  }
+  for (int a = blockIdx.y; a < natoms; a += gridDim.y)
+    dist[(int64_t)a * ld + p] = dist64(px, py, pz, coords + 3 * a);
 }
 
 __device__ __forceinline__ double ssf_s(double mu) {
@@ -91,8 +97,9 @@ __global__ void ssf_weights_kernel(int64_t npts, int natoms, const int32_t* __re
   weights[p] *= parent / sum;
 }
 // ---------------------------------------------------------------- screened kernel
-// Same weights, far fewer cell-product factors.  A warp takes 32 consecutive
-// points (a chunk; the points of one task are close together) and
+// Same weights, far fewer and far cheaper cell-product factors.  A warp
+// takes 32 consecutive points (a chunk; the points of one task are close
+// together) and
 //   * sorts the atoms by their distance d_B to the centre of the chunk's
 //     bounding box (bitonic sort of 32-bit (d_B, B) keys in shared memory), h being
 //     the chunk's radius, so that every point has r_B in [d_B - h, d_B + h];
@@ -103,13 +110,21 @@ __global__ void ssf_weights_kernel(int64_t npts, int natoms, const int32_t* __re
 //     order: the nearest atoms (the likely zero factors) come first, and the
 //     loop ends at the first atom with d_B - h >= r_A (1 + a) / (1 - a):
 //     from there on R_AB <= r_A + r_B gives mu_AB <= -a, a factor of exactly
-//     1 for every later atom.
+//     1 for every later atom;
+//   * classifies every factor first in FP32 (distances and R_AB from FP32
+//     coordinates relative to an origin o): mu_f <= -a - m means mu <= -a
+//     (factor exactly 1, skipped) and mu_f >= a + m means mu >= a (factor
+//     exactly 0), where the margin m bounds |mu_f - mu| (the caller derives
+//     it from the largest |x - o| of atoms and points and the smallest R_AB:
+//     FP32 rounding of coordinates, differences, squares and roots).  Only
+//     factors inside the switching band take the FP64 path: distances from
+//     dist64, mu = (r_A - r_B) / R_AB and s(mu) exactly as the reference.
 // The cell products follow the reference's rules: a zero factor ends the
 // product, and so does a product at or below 1e-13 (kept as it is).  Only
 // the order of the factors differs from cuda_ssf_1d.cu (nearest first instead
 // of atom index order); atoms dropped for the chunk contribute exactly 0.
 // Margins of 1e-9 on mu and of 1e-12 relative / 1e-10 bohr on h keep every
-// bound valid under FP64 rounding.
+// bound valid under FP64 rounding.  No distance table is needed.
 constexpr int kSSFWarps = 4;
 constexpr double kSSFFar = (1. + kSSFa) / (1. - kSSFa);
 
@@ -129,26 +144,42 @@ __device__ __forceinline__ double warp_max(double v) {
 // the key orders by distance and the key with the index bits cleared is a
 // lower bound of d_B.
 constexpr uint32_t kSSFIndexMask = 0x7FFu;
-__device__ __forceinline__ double key_dist(uint32_t key) {
-  return (double)__uint_as_float(key & ~kSSFIndexMask);
+__device__ __forceinline__ float key_dist(uint32_t key) {
+  return __uint_as_float(key & ~kSSFIndexMask);
 }
 
-// Cell product P_A at point p over the atoms in the chunk's distance order.
-__device__ __forceinline__ double cell_sorted(int A, int natoms, int64_t p, double h,
+// One point (FP64 p, FP32 q = p - o) as seen by the factor loops.
+struct SSFPoint {
+  double px, py, pz;
+  float qx, qy, qz;
+};
+
+// Cell product P_A at a point over the atoms in the chunk's distance order;
+// rA = dist64 of the point to A.
+__device__ __forceinline__ double cell_sorted(int A, double rA, int natoms, double h,
                                               const uint32_t* __restrict__ keys,
-                                              const double* __restrict__ dist, int ld,
-                                              const double* __restrict__ rab_inv, int ld_rab) {
-  const double rA = dist[(int64_t)A * ld + p];
-  const double* rinv = rab_inv + (int64_t)A * ld_rab;
+                                              const SSFPoint& pt, const double* __restrict__ coords,
+                                              const float4* __restrict__ cf,
+                                              const double* __restrict__ rinv, float margin) {
+  const float4 gA = cf[A];
+  const float rAf = (float)rA;
   // atoms with d_B >= lim have r_B >= kSSFFar r_A (1 + 1e-9): factor 1
-  const double lim = kSSFFar * rA * (1. + 1e-9) + h;
+  const float limf = __double2float_ru(kSSFFar * rA * (1. + 1e-9) + h);
+  const float lo = -(float)kSSFa - margin, hi = (float)kSSFa + margin;
   double ps = 1.;
   for (int k = 0; k < natoms; ++k) {
     const uint32_t key = keys[k];
-    if (key_dist(key) >= lim) break;
+    if (key_dist(key) >= limf) break;
     const int B = (int)(key & kSSFIndexMask);
     if (B == A) continue;
-    const double mu = (rA - dist[(int64_t)B * ld + p]) * rinv[B];
+    const float4 gB = cf[B];
+    const float dx = pt.qx - gB.x, dy = pt.qy - gB.y, dz = pt.qz - gB.z;
+    const float rBf = sqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
+    const float ex = gA.x - gB.x, ey = gA.y - gB.y, ez = gA.z - gB.z;
+    const float muf = (rAf - rBf) * rsqrtf(fmaf(ez, ez, fmaf(ey, ey, ex * ex)));
+    if (muf <= lo) continue;   // mu <= -a: factor exactly 1
+    if (muf >= hi) return 0.;  // mu >= a: factor exactly 0
+    const double mu = (rA - dist64(pt.px, pt.py, pt.pz, coords + 3 * B)) * rinv[B];
     if (mu >= kSSFa) return 0.;
     if (mu > -kSSFa) {
       ps *= ssf_s(mu);
@@ -163,8 +194,9 @@ __global__ void __launch_bounds__(kSSFWarps * 32)
                         const double* __restrict__ y, const double* __restrict__ z,
                         const int32_t* __restrict__ iparent,
                         const double* __restrict__ dist_nearest,
-                        const double* __restrict__ coords, const double* __restrict__ rab_inv,
-                        int ld_rab, const double* __restrict__ dist, int ld,
+                        const double* __restrict__ coords, const float4* __restrict__ cf,
+                        double ox, double oy, double oz, float margin,
+                        const double* __restrict__ rab_inv, int ld_rab,
                         double* __restrict__ weights, int* __restrict__ status) {
   extern __shared__ uint32_t ssf_smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -247,9 +279,12 @@ __global__ void __launch_bounds__(kSSFWarps * 32)
     if (status) atomicExch(status, 1);
     return;
   }
+  const SSFPoint pt{px, py, pz, (float)(px - ox), (float)(py - oy), (float)(pz - oz)};
+  const double rip = dist64(px, py, pz, coords + 3 * ip);
   const double cutoff = 0.5 * (1. - kSSFa) * dist_nearest[p];
-  if (dist[(int64_t)ip * ld + p] < cutoff) return;
-  const double parent = cell_sorted(ip, natoms, p, h, keys, dist, ld, rab_inv, ld_rab);
+  if (rip < cutoff) return;
+  const double parent = cell_sorted(ip, rip, natoms, h, keys, pt, coords, cf,
+                                    rab_inv + (int64_t)ip * ld_rab, margin);
   if (parent < DBL_EPSILON) {
     weights[p] = 0.;
     return;
@@ -258,7 +293,8 @@ __global__ void __launch_bounds__(kSSFWarps * 32)
   for (int c = 0; c < ncand; ++c) {
     const int A = cand[c];
     if (A == ip) continue;
-    sum += cell_sorted(A, natoms, p, h, keys, dist, ld, rab_inv, ld_rab);
+    sum += cell_sorted(A, dist64(px, py, pz, coords + 3 * A), natoms, h, keys, pt, coords, cf,
+                       rab_inv + (int64_t)A * ld_rab, margin);
   }
   weights[p] *= parent / sum;
 }
@@ -268,17 +304,11 @@ __global__ void __launch_bounds__(kSSFWarps * 32)
 void launch_ssf_weights_screened(int64_t npts, int natoms, const double* x, const double* y,
                                  const double* z, const int32_t* iparent,
                                  const double* dist_nearest, const double* coords,
-                                 const double* rab_inv, int ld_rab, double* dist_scr, int ld_dist,
-                                 double* weights, int* status, cudaStream_t s) {
+                                 const float4* coords_f, double ox, double oy, double oz,
+                                 float margin, const double* rab_inv, int ld_rab, double* weights,
+                                 int* status, cudaStream_t s) {
   if (npts == 0) return;
-  if (natoms > kSSFScreenedMaxAtoms) {
-    launch_ssf_weights(npts, natoms, x, y, z, iparent, dist_nearest, coords, rab_inv, ld_rab,
-                       dist_scr, ld_dist, weights, status, s);
-    return;
-  }
-  const int threads = 256;
-  dim3 g1((unsigned)((npts + threads - 1) / threads), (unsigned)std::min(natoms, 64));
-  grid_to_center_kernel<<<g1, threads, 0, s>>>(npts, natoms, x, y, z, coords, dist_scr, ld_dist);
+  if (natoms > kSSFScreenedMaxAtoms) throw std::runtime_error("screened SSF: more atoms than its sort keys can index");
   int nsort = 32;
   while (nsort < natoms) nsort <<= 1;
   const size_t smem = (size_t)kSSFWarps * (nsort + nsort / 2) * sizeof(uint32_t);
@@ -292,9 +322,9 @@ void launch_ssf_weights_screened(int64_t npts, int natoms, const double* x, cons
   }
   const int64_t chunks = (npts + 31) / 32;
   const unsigned blocks = (unsigned)((chunks + kSSFWarps - 1) / kSSFWarps);
-  ssf_screened_kernel<<<blocks, kSSFWarps * 32, smem, s>>>(npts, natoms, nsort, x, y, z, iparent,
-                                                           dist_nearest, coords, rab_inv, ld_rab,
-                                                           dist_scr, ld_dist, weights, status);
+  ssf_screened_kernel<<<blocks, kSSFWarps * 32, smem, s>>>(
+      npts, natoms, nsort, x, y, z, iparent, dist_nearest, coords, coords_f, ox, oy, oz, margin,
+      rab_inv, ld_rab, weights, status);
   GB300_CUDA(cudaGetLastError());
 }
 

@@ -6,6 +6,7 @@
 // into the tasks and marks the load balancer as weighted.  R_AB enters the
 // kernel inverted (send_static_data_weights, xc_device_stack_data.cxx:322-348).
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 
 #include "../host/device_api.hpp"
@@ -25,18 +26,55 @@ struct DevBuf {
   DevBuf& operator=(const DevBuf&) = delete;
 };
 
-// Runs the SSF kernel over npts points, in batches bounded by the distance scratch.
+// Runs the SSF kernel over npts points.  Up to kSSFScreenedMaxAtoms atoms:
+// the screened kernel in batches of up to 2^24 points, with the FP32 inputs
+// of its factor classification (atom coordinates relative to their centroid
+// o, and the margin on mu); larger molecules: the reference-order kernel in
+// batches bounded by its distance table.
 void ssf_batched(int64_t npts, int natoms, const double* x, const double* y, const double* z,
                  const int32_t* ip, const double* dn, const double* coords,
                  const std::vector<double>& rab_inv, double* w) {
   if (cuda_device_count() == 0) throw error("no CUDA device available for SSF weights");
   cudaStream_t s;
   GB300_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  const bool screened = natoms <= kSSFScreenedMaxAtoms;
   const int64_t max_scr_doubles = (int64_t)1 << 29;  // 4 GiB of distances per batch
-  const int64_t bsz = std::max<int64_t>(1, std::min<int64_t>(npts, max_scr_doubles / natoms));
+  const int64_t cap = screened ? ((int64_t)1 << 24) : max_scr_doubles / std::max(natoms, 1);
+  const int64_t bsz = std::max<int64_t>(1, std::min<int64_t>(npts, cap));
   DevBuf<double> dx(bsz), dy(bsz), dz(bsz), dw(bsz), ddn(bsz), dc(3 * natoms),
-      drab((size_t)natoms * natoms), dscr((size_t)bsz * natoms);
+      drab((size_t)natoms * natoms), dscr(screened ? 1 : (size_t)bsz * natoms);
   DevBuf<int32_t> dip(bsz), dstat(1);
+  DevBuf<float4> dcf(screened ? natoms : 1);
+  double o[3] = {0., 0., 0.};
+  float margin = 0.f;
+  if (screened) {
+    // |mu_f - mu| <= 2 (28 E 2^-24 / R_min + 2^-20): E the largest |x - o| of
+    // atoms and points, R_min the smallest interatomic distance (FP32
+    // rounding of the coordinates, of differences, squares and roots, and
+    // rsqrtf's 2 ulp), with a factor 2 to spare
+    for (int a = 0; a < natoms; ++a)
+      for (int k = 0; k < 3; ++k) o[k] += coords[3 * a + k] / natoms;
+    double e2 = 0.;
+    for (int a = 0; a < natoms; ++a) {
+      const double u = coords[3 * a] - o[0], v = coords[3 * a + 1] - o[1], t = coords[3 * a + 2] - o[2];
+      e2 = std::max(e2, u * u + v * v + t * t);
+    }
+    for (int64_t i = 0; i < npts; ++i) {
+      const double u = x[i] - o[0], v = y[i] - o[1], t = z[i] - o[2];
+      e2 = std::max(e2, u * u + v * v + t * t);
+    }
+    double rinv_max = 0.;
+    for (double r : rab_inv) rinv_max = std::max(rinv_max, r);
+    const double E = std::sqrt(e2) * (1. + 1e-6);
+    const double m = 2. * (28. * E * std::ldexp(1., -24) * rinv_max + std::ldexp(1., -20));
+    margin = (float)std::max(m, 1e-5);
+    std::vector<float4> cf(natoms);
+    for (int a = 0; a < natoms; ++a)
+      cf[a] = make_float4((float)(coords[3 * a] - o[0]), (float)(coords[3 * a + 1] - o[1]),
+                          (float)(coords[3 * a + 2] - o[2]), 0.f);
+    GB300_CUDA(cudaMemcpyAsync(dcf.p, cf.data(), natoms * sizeof(float4), cudaMemcpyHostToDevice, s));
+    GB300_CUDA(cudaStreamSynchronize(s));
+  }
   GB300_CUDA(cudaMemsetAsync(dstat.p, 0, sizeof(int), s));
   GB300_CUDA(cudaMemcpyAsync(dc.p, coords, 3 * natoms * sizeof(double), cudaMemcpyHostToDevice, s));
   GB300_CUDA(cudaMemcpyAsync(drab.p, rab_inv.data(), rab_inv.size() * sizeof(double),
@@ -50,8 +88,12 @@ void ssf_batched(int64_t npts, int natoms, const double* x, const double* y, con
     GB300_CUDA(cudaMemcpyAsync(dw.p, w + b, nd, cudaMemcpyHostToDevice, s));
     GB300_CUDA(cudaMemcpyAsync(ddn.p, dn + b, nd, cudaMemcpyHostToDevice, s));
     GB300_CUDA(cudaMemcpyAsync(dip.p, ip + b, n * sizeof(int32_t), cudaMemcpyHostToDevice, s));
-    launch_ssf_weights_screened(n, natoms, dx.p, dy.p, dz.p, dip.p, ddn.p, dc.p, drab.p, natoms,
-                                dscr.p, (int)n, dw.p, dstat.p, s);
+    if (screened)
+      launch_ssf_weights_screened(n, natoms, dx.p, dy.p, dz.p, dip.p, ddn.p, dc.p, dcf.p, o[0],
+                                  o[1], o[2], margin, drab.p, natoms, dw.p, dstat.p, s);
+    else
+      launch_ssf_weights(n, natoms, dx.p, dy.p, dz.p, dip.p, ddn.p, dc.p, drab.p, natoms, dscr.p,
+                         (int)n, dw.p, dstat.p, s);
     GB300_CUDA(cudaMemcpyAsync(w + b, dw.p, nd, cudaMemcpyDeviceToHost, s));
     GB300_CUDA(cudaStreamSynchronize(s));
   }
