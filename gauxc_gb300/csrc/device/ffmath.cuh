@@ -169,6 +169,21 @@ __device__ __forceinline__ double to_double_fast(float hi, float lo, int e2) {
                                           ((unsigned long long)eo << 52) | (unsigned long long)m));
 }
 
+// f * 2^e2 as a double, exactly: the float's fields are written into a
+// double bit pattern with integer operations only (no FP64 instruction).
+// Zero gives 0; subnormal or non-finite floats and results outside the
+// normal range take the exact routine.
+__device__ __forceinline__ double f2d_scaled(float f, int e2) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xFFu;
+  const unsigned eo = e + 896u + (unsigned)e2;  // biased exponent of the result
+  if (e - 1u < 254u && eo - 1u < 2046u)
+    return __hiloint2double((int)((b & 0x80000000u) | (eo << 20) | ((b >> 3) & 0xFFFFFu)),
+                            (int)(b << 29));
+  if ((b & 0x7FFFFFFFu) == 0u) return 0.0;
+  return to_double_cold(f, 0.f, e2);
+}
+
 // a + b for float-float values (hi, lo)
 __device__ __forceinline__ float2 add(float2 a, float2 b) {
   float s, e;

@@ -588,16 +588,16 @@ __global__ void __launch_bounds__(kThreads, 1)
           // S[i][j] = (phi^T Z + Z^T phi)[i][j] = 2^(ecz - 14) D: the strict
           // upper triangle (i < j, union indices) goes to A[i][j], the
           // diagonal as S[i][i] / 2, so that A + A^T is the block's VXC
-          // contribution.  Transposed through `scratch` (as doubles) for
-          // atomics along rows of A.
+          // contribution.  The float-float pairs are transposed through
+          // `scratch` for atomics along rows of A; hi and lo then enter A as
+          // two exact doubles, each made with integer operations (a single
+          // rounded double of hi + lo would take many more instructions, and
+          // GB300's FP64 pipe is throttled), with one FP64 atomic each.
           const int gm_l = bfl[i];
           const int gn_l = bfl[jc + (lane & 15)];
-          double* tr = reinterpret_cast<double*>(scratch);
 #pragma unroll
           for (int n = 0; n < 16; ++n)
-            tr[lane * 16 + (n ^ (lane & 15))] =
-                i <= jc + n ? ff::to_double_fast(hi[0][n], lo[0][n], ecz - 14 - (i == jc + n ? 1 : 0))
-                            : 0.;
+            scratch[lane * 16 + (n ^ (lane & 15))] = make_float2(hi[0][n], lo[0][n]);
           __syncwarp();
           const int n = lane & 15;
           const int gn = __shfl_sync(0xffffffffu, gn_l, n);
@@ -606,8 +606,13 @@ __global__ void __launch_bounds__(kThreads, 1)
             const int r2 = (lane >> 4) + 2 * t;
             const int im = it.m0 + qq * 32 + r2;
             const int gm = __shfl_sync(0xffffffffu, gm_l, r2);
-            if (im <= jc + n && gm >= 0 && gn >= 0)
-              atomicAdd(&out[(int64_t)gm * nbf + gn], tr[r2 * 16 + (n ^ (r2 & 15))]);
+            if (im <= jc + n && gm >= 0 && gn >= 0) {
+              const float2 v = scratch[r2 * 16 + (n ^ (r2 & 15))];
+              const int e2 = ecz - 14 - (im == jc + n ? 1 : 0);
+              double* dst = &out[(int64_t)gm * nbf + gn];
+              atomicAdd(dst, ff::f2d_scaled(v.x, e2));
+              atomicAdd(dst, ff::f2d_scaled(v.y, e2));
+            }
           }
           __syncwarp();
         }

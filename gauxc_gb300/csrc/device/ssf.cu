@@ -148,44 +148,120 @@ __device__ __forceinline__ float key_dist(uint32_t key) {
   return __uint_as_float(key & ~kSSFIndexMask);
 }
 
-// One point (FP64 p, FP32 q = p - o) as seen by the factor loops.
-struct SSFPoint {
-  double px, py, pz;
-  float qx, qy, qz;
+// Factors inside the switching band are not evaluated where the FP32 pass
+// finds them (a lane at a time, the other lanes of the warp idle on the
+// throttled FP64 pipe): each lane queues them, kSSFSlots at most, and the
+// warp evaluates every queued factor with all 32 lanes at once, then each
+// lane applies its own values in order.
+constexpr int kSSFSlots = 16;
+constexpr uint16_t kSSFZero = 0xFFFFu;  // queued factor that is exactly 0
+struct SSFWarpScratch {
+  double px[32], py[32], pz[32], rA[32];  // each lane's point and r_A of its cell
+  double s[32][kSSFSlots];                // values of the queued factors
+  int A[32], off[32];                     // each lane's cell atom, queue offsets
+  uint16_t b[32][kSSFSlots];              // queued atoms B (kSSFZero: factor 0)
 };
 
-// Cell product P_A at a point over the atoms in the chunk's distance order;
-// rA = dist64 of the point to A.
-__device__ __forceinline__ double cell_sorted(int A, double rA, int natoms, double h,
-                                              const uint32_t* __restrict__ keys,
-                                              const SSFPoint& pt, const double* __restrict__ coords,
-                                              const float4* __restrict__ cf,
-                                              const double* __restrict__ rinv, float margin) {
+// Evaluates every queued factor (all lanes), then lane by lane multiplies
+// its own in queue order into ps, applying the reference's stops: a product
+// at or below 1e-13 ends the cell (`done`), as does a zero factor.
+__device__ __forceinline__ void ssf_flush(SSFWarpScratch& ws, int lane, int& cnt, double& ps,
+                                          bool& done, const double* __restrict__ coords,
+                                          const double* __restrict__ rab_inv, int ld_rab) {
+  int incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  ws.off[lane] = incl - cnt;
+  __syncwarp();
+  for (int e = lane; e < total; e += 32) {
+    int lo = 0, hi = 31;  // the last lane whose queue starts at or before e
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (ws.off[mid] <= e) lo = mid; else hi = mid - 1;
+    }
+    const int L = lo, slot = e - ws.off[L];
+    const int B = ws.b[L][slot];
+    double v = 0.;
+    if (B != kSSFZero) {
+      const double mu = (ws.rA[L] - dist64(ws.px[L], ws.py[L], ws.pz[L], coords + 3 * B)) *
+                        rab_inv[(int64_t)ws.A[L] * ld_rab + B];
+      v = mu >= kSSFa ? 0. : (mu > -kSSFa ? ssf_s(mu) : 1.);
+    }
+    ws.s[L][slot] = v;
+  }
+  __syncwarp();
+  if (cnt > 0) {
+    // the factors are <= 1, so the product only decreases: when the whole
+    // queue leaves it above 1e-13 no stop was passed on the way
+    double q = ps;
+    for (int j = 0; j < cnt; ++j) q *= ws.s[lane][j];
+    if (q > kSSFTol) {
+      ps = q;
+    } else {
+      for (int j = 0; j < cnt; ++j) {
+        ps *= ws.s[lane][j];
+        if (ps <= kSSFTol) break;
+      }
+      done = true;
+    }
+  }
+  cnt = 0;
+  __syncwarp();
+}
+
+// Cell products P_A at the warp's points (warp-collective: every lane calls
+// it; `act` false leaves a lane out), the atoms in the chunk's distance order,
+// rA = dist64 of the lane's point to its A.
+__device__ __forceinline__ double cell_warp(bool act, int A, double rA, int natoms, double h,
+                                            const uint32_t* __restrict__ keys, float qx, float qy,
+                                            float qz, SSFWarpScratch& ws, int lane,
+                                            const double* __restrict__ coords,
+                                            const float4* __restrict__ cf,
+                                            const double* __restrict__ rab_inv, int ld_rab,
+                                            float margin) {
+  ws.A[lane] = A;
+  ws.rA[lane] = rA;
   const float4 gA = cf[A];
   const float rAf = (float)rA;
   // atoms with d_B >= lim have r_B >= kSSFFar r_A (1 + 1e-9): factor 1
   const float limf = __double2float_ru(kSSFFar * rA * (1. + 1e-9) + h);
   const float lo = -(float)kSSFa - margin, hi = (float)kSSFa + margin;
   double ps = 1.;
+  bool done = !act;
+  int cnt = 0;
   for (int k = 0; k < natoms; ++k) {
-    const uint32_t key = keys[k];
-    if (key_dist(key) >= limf) break;
-    const int B = (int)(key & kSSFIndexMask);
-    if (B == A) continue;
-    const float4 gB = cf[B];
-    const float dx = pt.qx - gB.x, dy = pt.qy - gB.y, dz = pt.qz - gB.z;
-    const float rBf = sqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
-    const float ex = gA.x - gB.x, ey = gA.y - gB.y, ez = gA.z - gB.z;
-    const float muf = (rAf - rBf) * rsqrtf(fmaf(ez, ez, fmaf(ey, ey, ex * ex)));
-    if (muf <= lo) continue;   // mu <= -a: factor exactly 1
-    if (muf >= hi) return 0.;  // mu >= a: factor exactly 0
-    const double mu = (rA - dist64(pt.px, pt.py, pt.pz, coords + 3 * B)) * rinv[B];
-    if (mu >= kSSFa) return 0.;
-    if (mu > -kSSFa) {
-      ps *= ssf_s(mu);
-      if (ps <= kSSFTol) break;
+    if (!done) {
+      const uint32_t key = keys[k];
+      if (key_dist(key) >= limf) {
+        done = true;
+      } else {
+        const int B = (int)(key & kSSFIndexMask);
+        if (B != A) {
+          const float4 gB = cf[B];
+          const float dx = qx - gB.x, dy = qy - gB.y, dz = qz - gB.z;
+          const float rBf = sqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
+          const float ex = gA.x - gB.x, ey = gA.y - gB.y, ez = gA.z - gB.z;
+          const float muf = (rAf - rBf) * rsqrtf(fmaf(ez, ez, fmaf(ey, ey, ex * ex)));
+          if (muf >= hi) {  // mu >= a: factor exactly 0
+            ws.b[lane][cnt++] = kSSFZero;
+            done = true;
+          } else if (!(muf <= lo)) {  // inside the band (mu <= -a: factor 1, skipped)
+            ws.b[lane][cnt++] = (uint16_t)B;
+          }
+        }
+      }
+    }
+    const bool all_done = __all_sync(0xffffffffu, done);
+    if (all_done || __any_sync(0xffffffffu, cnt == kSSFSlots)) {
+      ssf_flush(ws, lane, cnt, ps, done, coords, rab_inv, ld_rab);
+      if (all_done || __all_sync(0xffffffffu, done)) return ps;
     }
   }
+  ssf_flush(ws, lane, cnt, ps, done, coords, rab_inv, ld_rab);
   return ps;
 }
 
@@ -271,32 +347,41 @@ __global__ void __launch_bounds__(kSSFWarps * 32)
     ncand += __popc(m);
   }
   __syncwarp();
-  if (!act) return;
 
-  // ---- this lane's point (reference rules, cuda_ssf_1d.cu:61-128)
-  const int ip = iparent[p];
-  if (ip < 0 || ip >= natoms) {
+  // ---- the lanes' points (reference rules, cuda_ssf_1d.cu:61-128); every
+  // lane stays in the warp-collective cell evaluations, `live` marks the
+  // points still being weighted
+  SSFWarpScratch& ws = reinterpret_cast<SSFWarpScratch*>(
+      ssf_smem + (size_t)kSSFWarps * (nsort + nsort / 2))[warp];
+  int ip = act ? iparent[p] : 0;
+  bool live = act;
+  if (act && (ip < 0 || ip >= natoms)) {
     if (status) atomicExch(status, 1);
-    return;
+    live = false;
+    ip = 0;
   }
-  const SSFPoint pt{px, py, pz, (float)(px - ox), (float)(py - oy), (float)(pz - oz)};
+  ws.px[lane] = px;
+  ws.py[lane] = py;
+  ws.pz[lane] = pz;
+  const float qx = (float)(px - ox), qy = (float)(py - oy), qz = (float)(pz - oz);
   const double rip = dist64(px, py, pz, coords + 3 * ip);
-  const double cutoff = 0.5 * (1. - kSSFa) * dist_nearest[p];
-  if (rip < cutoff) return;
-  const double parent = cell_sorted(ip, rip, natoms, h, keys, pt, coords, cf,
-                                    rab_inv + (int64_t)ip * ld_rab, margin);
-  if (parent < DBL_EPSILON) {
+  if (live && rip < 0.5 * (1. - kSSFa) * dist_nearest[p]) live = false;
+  const double parent = cell_warp(live, ip, rip, natoms, h, keys, qx, qy, qz, ws, lane, coords,
+                                  cf, rab_inv, ld_rab, margin);
+  if (live && parent < DBL_EPSILON) {
     weights[p] = 0.;
-    return;
+    live = false;
   }
   double sum = parent;
   for (int c = 0; c < ncand; ++c) {
     const int A = cand[c];
-    if (A == ip) continue;
-    sum += cell_sorted(A, dist64(px, py, pz, coords + 3 * A), natoms, h, keys, pt, coords, cf,
-                       rab_inv + (int64_t)A * ld_rab, margin);
+    const bool use = live && A != ip;
+    if (!__any_sync(0xffffffffu, use)) continue;
+    const double v = cell_warp(use, A, dist64(px, py, pz, coords + 3 * A), natoms, h, keys, qx, qy,
+                               qz, ws, lane, coords, cf, rab_inv, ld_rab, margin);
+    if (use) sum += v;
   }
-  weights[p] *= parent / sum;
+  if (live) weights[p] *= parent / sum;
 }
 
 }  // namespace
@@ -311,13 +396,16 @@ void launch_ssf_weights_screened(int64_t npts, int natoms, const double* x, cons
   if (natoms > kSSFScreenedMaxAtoms) throw std::runtime_error("screened SSF: more atoms than its sort keys can index");
   int nsort = 32;
   while (nsort < natoms) nsort <<= 1;
-  const size_t smem = (size_t)kSSFWarps * (nsort + nsort / 2) * sizeof(uint32_t);
+  // per warp: nsort keys and nsort / 2 words of candidates (nsort >= 32, so
+  // 8-byte aligned), then the per-warp factor queues (SSFWarpScratch)
+  const size_t smem = (size_t)kSSFWarps * ((nsort + nsort / 2) * sizeof(uint32_t) +
+                                           sizeof(SSFWarpScratch));
   static bool attr = false;
   if (!attr) {
     GB300_CUDA(cudaFuncSetAttribute(
         ssf_screened_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-        (int)((size_t)kSSFWarps * (kSSFScreenedMaxAtoms + kSSFScreenedMaxAtoms / 2) *
-              sizeof(uint32_t))));
+        (int)((size_t)kSSFWarps * ((kSSFScreenedMaxAtoms + kSSFScreenedMaxAtoms / 2) *
+                                       sizeof(uint32_t) + sizeof(SSFWarpScratch)))));
     attr = true;
   }
   const int64_t chunks = (npts + 31) / 32;
