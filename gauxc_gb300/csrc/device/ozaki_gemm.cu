@@ -77,7 +77,7 @@ constexpr int kStageBytes = kABytes + kBBytes;
 constexpr uint32_t kTmemCols = 512;  // six levels x 64 columns (384) rounded up
 constexpr int kChunkBytes = 32 * 16 * 8;  // one unit's data: 32 rows x 16 columns, 8 bytes each
 constexpr int kWorkWarps = kEpiWarps - 2;  // draining warps that also process (not quarter 1)
-constexpr int kRedOffset = kStages * kStageBytes;  // per working warp: parked chunk / transposition
+constexpr int kRedOffset = kStages * kStageBytes;  // per working warp: a parked chunk
 constexpr int kHandOffset = kRedOffset + kWorkWarps * kChunkBytes;
 constexpr int kBarOffset = kHandOffset + 4 * kChunkBytes;  // the four quarter-1 chunks
 constexpr uint16_t kClusterMask = (1u << kCluster) - 1;
@@ -514,9 +514,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         break;
       }
       // density: the second chunk waits in shared memory while the first is
-      // processed (registers); VXC keeps it and uses `mine` to transpose
+      // processed (registers); VXC keeps it in registers
       if (!helper && EPI == EPI_X) put(mine, hi[1], lo[1]);
-      float2* scratch = helper ? hand + c0 * (kChunkBytes / 8) : mine;
       for (int k = 0; k < 2; ++k) {
         const int c = c0 + k;
         const int qq = helper ? 1 : q4;
@@ -586,35 +585,29 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
         } else {
           // S[i][j] = (phi^T Z + Z^T phi)[i][j] = 2^(ecz - 14) D: the strict
-          // upper triangle (i < j, union indices) goes to A[i][j], the
-          // diagonal as S[i][i] / 2, so that A + A^T is the block's VXC
-          // contribution.  The float-float pairs are transposed through
-          // `scratch` for atomics along rows of A; hi and lo then enter A as
-          // two exact doubles, each made with integer operations (a single
-          // rounded double of hi + lo would take many more instructions, and
-          // GB300's FP64 pipe is throttled), with one FP64 atomic each.
-          const int gm_l = bfl[i];
+          // upper triangle (i < j, union indices) and the diagonal as
+          // S[i][i] / 2 go to the accumulator, so that A + A^T is the block's
+          // VXC contribution.  Either triangle of A may hold an entry, so
+          // S[i][j] goes to A[bf(j)][bf(i)]: for a fixed column j the 32
+          // lanes (consecutive rows i) write consecutive addresses, and no
+          // transposition is needed.  hi and lo enter A as two exact
+          // doubles, each built from the float's fields with a few integer
+          // operations (f2d_scaled), with one FP64 atomic each: measured
+          // faster than one atomic of the rounded double of hi + lo, whose
+          // integer construction costs more than the second atomic (GB300's
+          // FP64 pipe is throttled, so no FP64 arithmetic is used here).
+          const int gm = bfl[i];
           const int gn_l = bfl[jc + (lane & 15)];
 #pragma unroll
-          for (int n = 0; n < 16; ++n)
-            scratch[lane * 16 + (n ^ (lane & 15))] = make_float2(hi[0][n], lo[0][n]);
-          __syncwarp();
-          const int n = lane & 15;
-          const int gn = __shfl_sync(0xffffffffu, gn_l, n);
-#pragma unroll
-          for (int t = 0; t < 16; ++t) {
-            const int r2 = (lane >> 4) + 2 * t;
-            const int im = it.m0 + qq * 32 + r2;
-            const int gm = __shfl_sync(0xffffffffu, gm_l, r2);
-            if (im <= jc + n && gm >= 0 && gn >= 0) {
-              const float2 v = scratch[r2 * 16 + (n ^ (r2 & 15))];
-              const int e2 = ecz - 14 - (im == jc + n ? 1 : 0);
-              double* dst = &out[(int64_t)gm * nbf + gn];
-              atomicAdd(dst, ff::f2d_scaled(v.x, e2));
-              atomicAdd(dst, ff::f2d_scaled(v.y, e2));
+          for (int n = 0; n < 16; ++n) {
+            const int gn = __shfl_sync(0xffffffffu, gn_l, n);
+            if (i <= jc + n && gm >= 0 && gn >= 0) {
+              const int e2 = ecz - 14 - (i == jc + n ? 1 : 0);
+              double* dst = &out[(int64_t)gn * nbf + gm];
+              atomicAdd(dst, ff::f2d_scaled(hi[0][n], e2));
+              atomicAdd(dst, ff::f2d_scaled(lo[0][n], e2));
             }
           }
-          __syncwarp();
         }
         clear(hi[0], lo[0]);
       }
@@ -876,11 +869,14 @@ double ozaki_selftest(int n, int k) {
       S[(size_t)a * n + b] = acc;
       smax = std::max(smax, std::fabs(acc));
     }
+  // the accumulator may hold an entry in either triangle: compare A + A^T
+  // with the symmetric product
   double worst = 0.;
   for (int a = 0; a < n; ++a)
     for (int b = 0; b < n; ++b) {
-      const double ref = b > a ? S[(size_t)a * n + b] : (b == a ? 0.5 * S[(size_t)a * n + a] : 0.);
-      worst = std::max(worst, std::fabs(C[(size_t)a * n + b] - ref) / std::max(smax, 1e-300));
+      const double ref = S[(size_t)std::min(a, b) * n + std::max(a, b)];
+      const double got = C[(size_t)a * n + b] + C[(size_t)b * n + a];
+      worst = std::max(worst, std::fabs(got - ref) / std::max(smax, 1e-300));
     }
   return worst;
 }
