@@ -65,6 +65,11 @@ def tensor_core_selftest(n=256, k=256):
     return float(_call(_L.gauxc_gb300_tensor_core_selftest, int(n), int(k)))
 
 
+def ff_exp_selftest(n=1 << 20):
+    """Largest relative error of the collocation's float-float exp against FP64."""
+    return float(_call(_L.gauxc_gb300_ff_exp_selftest, int(n)))
+
+
 def host_register(a):
     """Page-locks the memory of numpy array `a` in place (for P / VXC buffers
     reused every SCF iteration); True when it registered it."""

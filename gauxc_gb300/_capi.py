@@ -148,6 +148,7 @@ PROTOTYPES = {
     "gauxc_gb300_host_unregister": (None, [S, ctypes.c_void_p]),
     "gauxc_gb300_set_device": (None, [S, I]),
     "gauxc_gb300_tensor_core_selftest": (dbl, [S, I, I]),
+    "gauxc_gb300_ff_exp_selftest": (dbl, [S, I]),
     "gauxc_gb300_ssf_weights": (None, [S, i64, i32, P(dbl), P(i32), P(dbl), P(dbl), P(dbl)]),
     "gauxc_gb300_ssf_weights_noalloc": (None, [S, i64, i32, vp, vp, vp, vp, vp, vp, vp, vp]),
     "gauxc_gb300_collocation": (None, [S, GauXCBasisSet, i64, P(dbl), i32, P(i32), P(dbl),

@@ -17,6 +17,10 @@
 // digits need about 44 significant bits: FP32 instructions then replace the
 // FP64 ones of exp and of the angular polynomials, GB300's FP64 pipe being
 // about 64 times slower than its FP32 pipe.
+#include <cmath>
+#include <cstring>
+#include <type_traits>
+
 #include "device_common.cuh"
 #include "ffmath.cuh"
 #include "xc_mixed.cuh"
@@ -88,13 +92,21 @@ __device__ __forceinline__ void eval_shell(int l, int pure, V x, V y, V z, V R, 
 // a shell outside the point's own task list contributes exact zeros, so the
 // merged block reproduces the per-task screening of the reference.
 // exp(-a r2) in the value type's arithmetic
-__device__ __forceinline__ double exp_neg_v(double x) { return exp(x); }
-__device__ __forceinline__ ff::ffl exp_neg_v(ff::ffl x) { return ff::exp_neg(x); }
+__device__ __forceinline__ double exp_neg_v(double x, const float2*) { return exp(x); }
+__device__ __forceinline__ ff::ffl exp_neg_v(ff::ffl x, const float2* tab) {
+  return ff::exp_neg(x, tab);
+}
 
 template <bool GRAD, bool MASK, typename V>
 __global__ void __launch_bounds__(128) collocation_kernel(ShellsDev sh, TasksDev tk, PBMaskDev mk,
                                                           const int2* __restrict__ items,
                                                           double* __restrict__ scr) {
+  // float-float path: the table of 2^(j/32) in shared memory
+  __shared__ float2 tab[32];
+  if constexpr (!std::is_same<V, double>::value) {
+    if (threadIdx.x < 32) tab[threadIdx.x] = sh.exp2_tab[threadIdx.x];
+    __syncthreads();
+  }
   const int2 it = items[blockIdx.x];
   const int t = it.x;
   const int p = it.y * blockDim.x + threadIdx.x;
@@ -137,7 +149,7 @@ __global__ void __launch_bounds__(128) collocation_kernel(ShellsDev sh, TasksDev
     V R = zero, R1 = zero;
     for (int k = sh.prim_off[s]; k < sh.prim_off[s + 1]; ++k) {
       const V a = V(sh.alpha[k]);
-      const V e = V(sh.coeff[k]) * exp_neg_v(-(a * r2));
+      const V e = V(sh.coeff[k]) * exp_neg_v(-(a * r2), tab);
       R = R + e;
       if (GRAD) R1 = R1 + a * e;
     }
@@ -180,6 +192,55 @@ void launch_collocation(const ShellsDev& sh, const TasksDev& tk, const int2* ite
   else
     collocation_kernel<false, false, double><<<nitems, 128, 0, s>>>(sh, tk, none, items, scr);
   GB300_CUDA(cudaGetLastError());
+}
+
+std::vector<float2> exp2_table() {
+  std::vector<float2> t(32);
+  for (int j = 0; j < 32; ++j) {
+    const double v = std::exp2(j / 32.);
+    const float hi = (float)v;
+    t[j] = make_float2(hi, (float)(v - (double)hi));
+  }
+  return t;
+}
+
+namespace {
+// exp_neg against FP64 exp on n points spread over [-50, 0]: largest relative
+// error, as the bits of a non-negative double (atomicMax on the bit pattern)
+__global__ void exp_neg_selftest_kernel(int n, const float2* __restrict__ gtab,
+                                        unsigned long long* __restrict__ worst) {
+  __shared__ float2 tab[32];
+  if (threadIdx.x < 32) tab[threadIdx.x] = gtab[threadIdx.x];
+  __syncthreads();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double x = -50. * (double)i / (double)(n - 1) - 1e-3 * (double)(i % 7);
+    const ff::ffl xf(x);
+    const ff::ffl y = ff::exp_neg(xf, tab);
+    const double ref = exp((double)xf.hi + (double)xf.lo);
+    const double err = fabs(((double)y.hi + (double)y.lo) - ref) / ref;
+    atomicMax(worst, (unsigned long long)__double_as_longlong(err));
+  }
+}
+}  // namespace
+
+double ff_exp_selftest(int n) {
+  if (n < 2) throw std::runtime_error("ff_exp_selftest: n < 2");
+  const std::vector<float2> t = exp2_table();
+  float2* dtab = nullptr;
+  unsigned long long* dw = nullptr;
+  GB300_CUDA(cudaMalloc(&dtab, 32 * sizeof(float2)));
+  GB300_CUDA(cudaMalloc(&dw, sizeof(unsigned long long)));
+  GB300_CUDA(cudaMemcpy(dtab, t.data(), 32 * sizeof(float2), cudaMemcpyHostToDevice));
+  GB300_CUDA(cudaMemset(dw, 0, sizeof(unsigned long long)));
+  exp_neg_selftest_kernel<<<(n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024, 256>>>(n, dtab, dw);
+  GB300_CUDA(cudaGetLastError());
+  unsigned long long w = 0;
+  GB300_CUDA(cudaMemcpy(&w, dw, sizeof(w), cudaMemcpyDeviceToHost));
+  cudaFree(dtab);
+  cudaFree(dw);
+  double r;
+  std::memcpy(&r, &w, sizeof(r));
+  return r;
 }
 
 void launch_collocation_masked(const ShellsDev& sh, const TasksDev& tk, const PBMaskDev& mk,

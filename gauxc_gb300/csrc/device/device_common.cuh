@@ -5,6 +5,7 @@
 #include <cstdint>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #ifndef GB300_HD
 #define GB300_HD __host__ __device__
@@ -29,7 +30,14 @@ struct ShellsDev {
   const double* origin;   // [3*nshells]
   const int* l;           // angular momentum
   const int* pure;        // 1 = spherical
+  // 2^(j/32), j = 0..31, as float-float pairs (exp2_table; the float-float
+  // collocation of the tensor-core path only)
+  const float2* exp2_tab = nullptr;
 };
+
+// The 32 values 2^(j/32) as float-float pairs (hi = the float nearest the
+// double, lo = the float nearest the remainder), for ff::exp_neg.
+std::vector<float2> exp2_table();
 
 // Per-task layout of the device-resident plan (all device pointers).
 // Points of task t live at [pt_off[t], pt_off[t] + npts_pad[t]); tasks are

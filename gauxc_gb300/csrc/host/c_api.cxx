@@ -902,6 +902,16 @@ double gauxc_gb300_tensor_core_selftest(GauXCStatus* status, int n, int k) {
   return r;
 }
 
+double gauxc_gb300_ff_exp_selftest(GauXCStatus* status, int n) {
+  status_init(status);
+  double r = -1.;
+  guarded(status, [&] {
+    if (cuda_device_count() == 0) throw error("no CUDA device available");
+    r = ff_exp_selftest(n);
+  });
+  return r;
+}
+
 void gauxc_gb300_set_device(GauXCStatus* status, int device) {
   status_init(status);
   guarded(status, [&] { set_device(device); });

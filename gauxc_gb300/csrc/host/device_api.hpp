@@ -108,6 +108,9 @@ bool host_register(void* p, size_t bytes);
 void host_unregister(void* p);
 // Tensor-core emulated-FP64 GEMM self-test: worst relative error.
 double tensor_core_selftest(int n, int k);
+// Largest relative error of the float-float exp of the collocation over n
+// points of [-50, 0] against FP64 exp.
+double ff_exp_selftest(int n);
 void set_device(int dev);
 
 // Collision bitset of task boxes (6 doubles each: lo xyz, up xyz) against the

@@ -320,6 +320,9 @@ void gauxc_gb300_host_unregister(GauXCStatus* status, void* ptr);
    64, k <= 256) against FP64; returns the worst error relative to the largest
    output element. */
 double gauxc_gb300_tensor_core_selftest(GauXCStatus* status, int n, int k);
+/* Self-test of the float-float exp of the tensor-core path's collocation:
+   the largest relative error against FP64 exp over n points of [-50, 0]. */
+double gauxc_gb300_ff_exp_selftest(GauXCStatus* status, int n);
 /* cudaSetDevice for the calling thread (one process per GPU). */
 void gauxc_gb300_set_device(GauXCStatus* status, int device);
 

@@ -22,6 +22,13 @@ def test_tensor_core_gemm_selftest(g, n, k):
     assert g.tensor_core_selftest(n, k) <= 1e-11
 
 
+def test_float_float_exp_selftest(g):
+    # table-driven exp of the collocation (Tang's method, 2^(j/32) table,
+    # degree-5 polynomial on |r| <= ln2/64): about 2^-46 relative; the
+    # float-float input itself carries 2^-48 of |x| <= 50
+    assert g.ff_exp_selftest() <= 1e-13
+
+
 def _integrator(g, lb, func, lwd):
     mw = g.MolecularWeightsFactory(g.ExecutionSpace.Device).get_instance()
     if not lb.weights_modified():
