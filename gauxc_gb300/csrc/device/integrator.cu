@@ -276,6 +276,7 @@ void DeviceIntegrator::build(const LoadBalancer& lb) {
     sh_.origin = arena_.upload(o, s);
     sh_.l = arena_.upload(l, s);
     sh_.pure = arena_.upload(pure, s);
+    sh_.exp2_tab = arena_.upload(exp2_table(), s);
   }
 
   P_ = arena_.alloc<double>((size_t)nbf_ * nbf_);
@@ -483,11 +484,6 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
     std::vector<int> shells;  // sorted union
     int nu = 0, npts = 0;
   };
-  auto nbe_of = [&](const std::vector<int>& sl) {
-    int n = 0;
-    for (int x : sl) n += bs.shells[x].size();
-    return n;
-  };
   const int maxp = std::max(kNTile, std::min(kPBMaxPts, params_.pb_max_pts / kNTile * kNTile));
   const double w2 = std::max(0., params_.nu2_weight);
   // Task order of the merge: along a Morton curve of the tasks' centroids
@@ -524,37 +520,88 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
     std::iota(torder.begin(), torder.end(), 0);
     std::stable_sort(torder.begin(), torder.end(), [&](int x, int y) { return key[x] < key[y]; });
   }
+  // Merge: each task (piece) joins the cheapest of the last kMergeWindow
+  // blocks with room for its points, if that does not raise the cost, else
+  // it opens a block.  The open blocks' shell sets are bitsets; the union's
+  // basis size is nu(b) + nbe(t) - nbe(b & t), the intersection counted per
+  // shell size class with popcounts.  On 256 waters (CPU model) the window of
+  // 8 gives 40k blocks and 35 % less sum nu^2 than joining only the last
+  // block, for 3 % less tensor work.
+  constexpr int kMergeWindow = 8;
+  const int nsh_all = (int)bs.shells.size();
+  const int nw = (nsh_all + 63) / 64;
+  std::vector<int> csize;                     // distinct shell sizes
+  std::vector<std::vector<uint64_t>> cmask;   // shells of each size, as bitsets
+  for (int x = 0; x < nsh_all; ++x) {
+    const int sz = bs.shells[x].size();
+    size_t c = 0;
+    while (c < csize.size() && csize[c] != sz) ++c;
+    if (c == csize.size()) {
+      csize.push_back(sz);
+      cmask.emplace_back(nw, 0ull);
+    }
+    cmask[c][x >> 6] |= 1ull << (x & 63);
+  }
+  auto common_nbe = [&](const std::vector<uint64_t>& a, const std::vector<uint64_t>& b) {
+    int n = 0;
+    for (size_t c = 0; c < csize.size(); ++c) {
+      int k = 0;
+      for (int i = 0; i < nw; ++i) k += __builtin_popcountll(a[i] & b[i] & cmask[c][i]);
+      n += k * csize[c];
+    }
+    return n;
+  };
+  struct OpenPB {
+    int pb;
+    std::vector<uint64_t> bits;
+  };
   std::vector<PB> pbs;
+  std::vector<OpenPB> win;  // the last kMergeWindow blocks, oldest first
+  auto close_oldest = [&]() {
+    PB& b = pbs[win.front().pb];
+    b.shells.clear();
+    for (int i = 0; i < nw; ++i)
+      for (uint64_t w = win.front().bits[i]; w; w &= w - 1) b.shells.push_back(i * 64 + __builtin_ctzll(w));
+    win.erase(win.begin());
+  };
+  std::vector<uint64_t> tb(nw);
   for (int t : torder) {
     const XCTask& tt = tasks[t];
+    std::fill(tb.begin(), tb.end(), 0ull);
+    for (int x : tt.shell_list) tb[x >> 6] |= 1ull << (x & 63);
     for (int p0 = 0; p0 < tt.npts; p0 += maxp) {
-      const int p1 = std::min(tt.npts, p0 + maxp);
-      bool merged = false;
-      if (!pbs.empty() && pbs.back().npts + (p1 - p0) <= maxp) {
-        PB& b = pbs.back();
-        std::vector<int> u;
-        std::set_union(b.shells.begin(), b.shells.end(), tt.shell_list.begin(),
-                       tt.shell_list.end(), std::back_inserter(u));
-        const int nu = nbe_of(u);
-        if (pb_cost(b.npts + (p1 - p0), nu, w2) <=
-            pb_cost(b.npts, b.nu, w2) + pb_cost(p1 - p0, tt.nbe, w2)) {
-          b.shells.swap(u);
-          b.nu = nu;
-          b.npts += p1 - p0;
-          b.segs.push_back({t, p0, p1});
-          merged = true;
+      const int p1 = std::min(tt.npts, p0 + maxp), n = p1 - p0;
+      int best = -1, best_nu = 0;
+      double best_d = 0.;
+      for (int w = (int)win.size() - 1; w >= 0; --w) {
+        const PB& b = pbs[win[w].pb];
+        if (b.npts + n > maxp) continue;
+        const int nu = b.nu + tt.nbe - common_nbe(win[w].bits, tb);
+        const double d = pb_cost(b.npts + n, nu, w2) - pb_cost(b.npts, b.nu, w2) - pb_cost(n, tt.nbe, w2);
+        if (d <= best_d) {
+          best = w;
+          best_d = d;
+          best_nu = nu;
         }
       }
-      if (!merged) {
+      if (best >= 0) {
+        PB& b = pbs[win[best].pb];
+        for (int i = 0; i < nw; ++i) win[best].bits[i] |= tb[i];
+        b.nu = best_nu;
+        b.npts += n;
+        b.segs.push_back({t, p0, p1});
+      } else {
         PB b;
         b.segs.push_back({t, p0, p1});
-        b.shells.assign(tt.shell_list.begin(), tt.shell_list.end());
         b.nu = tt.nbe;
-        b.npts = p1 - p0;
+        b.npts = n;
         pbs.push_back(std::move(b));
+        win.push_back(OpenPB{(int)pbs.size() - 1, tb});
+        if ((int)win.size() > kMergeWindow) close_oldest();
       }
     }
   }
+  while (!win.empty()) close_oldest();
   // Blocks stay in the merge's spatial order: the VXC updates of neighbouring
   // blocks then hit the same rows and columns of the nbf x nbf accumulator
   // while they are resident in L2, and P's rows are gathered from L2 likewise.
@@ -569,7 +616,6 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
   // runs per radius, and the P gather and the VXC atomics touch fewer DRAM
   // sectors.  P_ and A_ live in this order; P comes in and VXC goes out
   // through permuting copies.
-  const int nsh_all = (int)bs.shells.size();
   std::vector<int> shell_pos(nsh_all), new_off(nsh_all);
   {
     double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
@@ -619,6 +665,7 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
   std::vector<int> npts_pad(npb), nk(npb), nu(npb), nu_pad(npb), nsh(npb), bf_list, sh_list,
       sh_col, member;
   std::vector<uint8_t> mask;
+  std::vector<uint64_t> mbits(nw, 0ull);  // a member task's shells (cleared after use)
   std::vector<double> X, Y, Z, W;
   stats = PlanStats{};
   int64_t pts = 0;
@@ -648,8 +695,9 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
     mask_off[i] = (int64_t)mask.size();
     for (size_t m = 0; m < b.segs.size(); ++m) {
       const XCTask& tt = tasks[b.segs[m].task];
-      for (int x : ushells)
-        mask.push_back(std::binary_search(tt.shell_list.begin(), tt.shell_list.end(), x) ? 1 : 0);
+      for (int x : tt.shell_list) mbits[x >> 6] |= 1ull << (x & 63);
+      for (int x : ushells) mask.push_back((uint8_t)((mbits[x >> 6] >> (x & 63)) & 1ull));
+      for (int x : tt.shell_list) mbits[x >> 6] = 0ull;
     }
     int np_real = 0;
     for (size_t m = 0; m < b.segs.size(); ++m) {
