@@ -1366,7 +1366,7 @@ double integrator_autotune(XCIntegratorHandle& h, const double* P, int64_t ldp, 
   std::vector<PlanParams> cands;
   if (h.prec == Precision::Mixed) {
     for (int pts : {128, 192, 256})
-      for (double w : {150., 300.}) cands.push_back(PlanParams{pts, w, h.params.scratch_bytes});
+      for (double w : {75., 150.}) cands.push_back(PlanParams{pts, w, h.params.scratch_bytes});
   } else {
     cands.push_back(h.params);
   }

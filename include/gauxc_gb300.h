@@ -369,7 +369,7 @@ void gauxc_gb300_collocation(GauXCStatus* status, const GauXCBasisSet basis, int
 void gauxc_gb300_integrator_set_plan_params(GauXCStatus* status, const GauXCIntegrator integrator,
                                             int pb_max_pts, double nu2_weight, double scratch_gb);
 /* Autotuner: builds and times one call per candidate plan (point-block sizes
-   128/192/256 x merge weights 150/300 for "GB300-Mixed"; the current plan
+   128/192/256 x merge weights 75/150 for "GB300-Mixed"; the current plan
    otherwise) on density P and keeps the fastest.  Returns its compute time in
    ms and the chosen parameters. */
 double gauxc_gb300_integrator_autotune(GauXCStatus* status, const GauXCIntegrator integrator,
