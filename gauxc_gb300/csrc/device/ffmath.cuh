@@ -140,33 +140,9 @@ __device__ __forceinline__ double to_double(float hi, float lo, int e2) {
   return __longlong_as_double((long long)(sign | ((unsigned long long)be << 52) | (M & 0xFFFFFFFFFFFFFULL)));
 }
 
-// Exact conversion as a separate function, the cold path of to_double_fast.
+// Exact conversion as a separate function, the cold path of f2d_scaled.
 static __device__ __noinline__ double to_double_cold(float hi, float lo, int e2) {
   return to_double(hi, lo, e2);
-}
-
-// (hi + lo) * 2^e2 for a float-float value with |lo| well below |hi| (as left by
-// two_sum chains): |hi| is written as a double bit pattern and lo, in units of
-// that double's last place (rounded to nearest), is added to the pattern.
-// Whenever that could leave hi's binade, or hi is zero, subnormal or not
-// finite, or the result leaves the normal range, the exact routine is used.
-__device__ __forceinline__ double to_double_fast(float hi, float lo, int e2) {
-  const unsigned hb = __float_as_uint(hi), lb = __float_as_uint(lo);
-  const int eh = (int)((hb >> 23) & 0xFF), el = (int)((lb >> 23) & 0xFF);
-  const int sh = el - eh + 29;  // lo / ulp = mant(lo) * 2^sh
-  const int eo = eh + 896 + e2;  // biased double exponent of the result
-  if (eh == 0 || eh == 0xFF || sh > 29 || eo <= 0 || eo >= 2047) return to_double_cold(hi, lo, e2);
-  const unsigned long long mh = (unsigned long long)(hb & 0x7FFFFFu) << 29;
-  long long L = 0;
-  if (el != 0 && sh > -26) {
-    const long long ml = (long long)((lb & 0x7FFFFFu) | 0x800000u);
-    L = sh >= 0 ? (ml << sh) : ((ml + (1LL << (-sh - 1))) >> (-sh));
-    if ((lb ^ hb) >> 31) L = -L;
-  }
-  const long long m = (long long)mh + L;  // stays in [0, 2^52) unless a binade is crossed
-  if (m < 0 || m >= (1LL << 52)) return to_double_cold(hi, lo, e2);
-  return __longlong_as_double((long long)(((unsigned long long)(hb >> 31) << 63) |
-                                          ((unsigned long long)eo << 52) | (unsigned long long)m));
 }
 
 // f * 2^e2 as a double, exactly: the float's fields are written into a

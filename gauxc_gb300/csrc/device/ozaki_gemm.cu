@@ -580,7 +580,9 @@ __global__ void __launch_bounds__(kThreads, 1)
             if ((lane & 1) == 0) {
               const int n = ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 +
                             ((lane >> 1) & 1);
-              atomicAdd(&out[4 * (gpt + c * 16 + n) + q], ff::to_double_fast(h[0], l[0], 0));
+              double* dst = &out[4 * (gpt + c * 16 + n) + q];
+              atomicAdd(dst, ff::f2d_scaled(h[0], 0));
+              atomicAdd(dst, ff::f2d_scaled(l[0], 0));
             }
           }
         } else {
