@@ -560,6 +560,7 @@ def main():
     t0 = time.perf_counter()
     eval_into(integ, P, V)
     t_first = time.perf_counter() - t0
+    plan_ms = {k: v for k, v in integ.timings().items() if k.startswith("plan")}
     for _ in range(args.warmup - 1):
         eval_into(integ, P, V)
     stats = integ.plan_stats()
@@ -700,7 +701,7 @@ def main():
         fp64_check=fp64_check, exc=exc, nel=nel, batched=batched,
         grid_points_bf_per_s=s1 / value, kernels=kernels,
         setup_s=dict(load_balancer=ctx["t_lb"], ssf_weights=ctx["t_w"],
-                     plan_build_and_first_call=t_first),
+                     plan_build_and_first_call=t_first, plan_ms=plan_ms),
         timed_wall_s=t_all)
     print(json.dumps(line), flush=True)
     return 0

@@ -450,9 +450,10 @@ class XCIntegrator(_Handle):
         return float(_call(_L.gauxc_gb300_integrator_last_nel, self._h))
 
     def timings(self):
-        out = (ctypes.c_double * 4)()
-        _call(_L.gauxc_gb300_integrator_timings, self._h, out, 4)
-        return dict(zip(["h2d_ms", "compute_ms", "d2h_ms", "wall_ms"], list(out)))
+        out = (ctypes.c_double * 8)()
+        _call(_L.gauxc_gb300_integrator_timings, self._h, out, 8)
+        return dict(zip(["h2d_ms", "compute_ms", "d2h_ms", "wall_ms", "plan_ms", "plan_merge_ms",
+                         "plan_layout_ms", "plan_lists_ms"], list(out)))
 
     def set_profiling(self, on=True):
         _call(_L.gauxc_gb300_integrator_set_profiling, self._h, ctypes.c_bool(on))

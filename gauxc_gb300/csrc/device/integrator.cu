@@ -286,9 +286,11 @@ void DeviceIntegrator::build(const LoadBalancer& lb) {
   err_ = arena_.alloc<int>(1);
   GB300_CUDA(cudaMemsetAsync(err_, 0, sizeof(int), s));
   if (prec_ == Precision::Mixed) {
+    const auto t0 = std::chrono::steady_clock::now();
     build_mixed(lb);
     if (func_.polarized) ensure_uks();
     GB300_CUDA(cudaStreamSynchronize(s));
+    timings["plan_ms"] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     generation = lb.generation;
     return;
   }
@@ -473,6 +475,10 @@ static double pb_cost(int npts, int nu, double nu2_weight) {
 // union-size term does not exceed that of its parts kept apart; a task larger
 // than kPBMaxPts points is split.  Padded extents: PBDims.
 void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
+  const auto t_plan0 = std::chrono::steady_clock::now();
+  auto ms_since = [](std::chrono::steady_clock::time_point a) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - a).count();
+  };
   const BasisSet& bs = *lb.basis;
   cudaStream_t s = stream_;
   const auto& tasks = lb.tasks;
@@ -608,6 +614,8 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
   std::vector<int> order(pbs.size());
   std::iota(order.begin(), order.end(), 0);
 
+  timings["plan_merge_ms"] = ms_since(t_plan0);
+  const auto t_layout0 = std::chrono::steady_clock::now();
   // Device AO order.  A block's union basis holds, for every cutoff radius,
   // the shells of that radius whose centres lie within reach of its points:
   // in the caller's order (atom by atom) that is a patchwork of short shell
@@ -746,6 +754,8 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
   stats.ntasks = (int64_t)tasks.size();
   stats.npts_pad = pts;
 
+  timings["plan_layout_ms"] = ms_since(t_layout0);
+  const auto t_lists0 = std::chrono::steady_clock::now();
   // ---- batches under the workspace budget
   size_t free_b = 0, total_b = 0;
   GB300_CUDA(cudaMemGetInfo(&free_b, &total_b));
@@ -882,6 +892,7 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
   zcoef_ = arena_.alloc<double4>(std::max<int64_t>(pts, 1));
   ndens_ = (int)mbatches_.size() * nfb;
   partials_ = arena_.alloc<double2>(std::max(ndens_, 1));
+  timings["plan_lists_ms"] = ms_since(t_lists0);
 }
 
 int64_t DeviceIntegrator::eval_mixed_batches(bool do_vxc) {

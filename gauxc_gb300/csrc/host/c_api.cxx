@@ -734,9 +734,10 @@ int gauxc_gb300_integrator_timings(GauXCStatus* status, const GauXCIntegrator in
   status_init(status);
   if (!check(status, integrator, GauXC_Type_Integrator, "Integrator")) return 0;
   auto t = integrator_timings(*deref<XCIntegratorHandle>(integrator.ptr));
-  const double v[4] = {t["h2d_ms"], t["compute_ms"], t["d2h_ms"], t["wall_ms"]};
+  const double v[8] = {t["h2d_ms"], t["compute_ms"], t["d2h_ms"], t["wall_ms"],
+                       t["plan_ms"], t["plan_merge_ms"], t["plan_layout_ms"], t["plan_lists_ms"]};
   int n = 0;
-  for (; n < 4 && n < nmax; ++n) out[n] = v[n];
+  for (; n < 8 && n < nmax; ++n) out[n] = v[n];
   return n;
 }
 

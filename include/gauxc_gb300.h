@@ -276,7 +276,10 @@ GauXCLoadBalancer gauxc_gb300_load_balancer_subset(GauXCStatus* status, const Ga
 
 /* N_el (integral of the total density) of the last eval_exc_vxc call. */
 double gauxc_gb300_integrator_last_nel(GauXCStatus* status, const GauXCIntegrator integrator);
-/* Timings of the last call in ms: {h2d, compute, d2h, wall}; returns the count written. */
+/* Timings in ms: {h2d, compute, d2h, wall} of the last call, then the
+   device plan's host build {total, merge of tasks into point blocks, layout,
+   work lists and uploads} (the plan is built by the first call after the
+   load balancer's weights change); returns the count written (<= 8). */
 int gauxc_gb300_integrator_timings(GauXCStatus* status, const GauXCIntegrator integrator,
                                    double* out, int nmax);
 /* Plan statistics: {ntasks, npts, npts_pad, nbatches, sum npts*nbe, sum npts*nbe^2,

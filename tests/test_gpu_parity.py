@@ -1,6 +1,6 @@
 """Device path against the oracle and the reference goldens (needs a GB300).
 
-Gates (spec tolerances for the plain FP64 path):
+Gates (the target tolerances of the plain FP64 path):
   |dEXC| <= 1e-10 Eh and max |dVXC_ij| <= 1e-10 against the FP64 oracle,
   SSF weights and collocation to ~1e-13 relative, task maps bit-exact.
 """
