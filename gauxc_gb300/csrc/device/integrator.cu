@@ -19,6 +19,7 @@
 #include <cstring>
 #include <numeric>
 #include <iterator>
+#include <thread>
 
 #include "../host/device_api.hpp"
 #include "device_common.cuh"
@@ -487,11 +488,63 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
   };
   struct PB {
     std::vector<Seg> segs;
-    std::vector<int> shells;  // sorted union
+    std::vector<int> shells;  // union, in device AO order
     int nu = 0, npts = 0;
   };
   const int maxp = std::max(kNTile, std::min(kPBMaxPts, params_.pb_max_pts / kNTile * kNTile));
   const double w2 = std::max(0., params_.nu2_weight);
+  // Device AO order.  A block's union basis holds, for every cutoff radius,
+  // the shells of that radius whose centres lie within reach of its points:
+  // in the caller's order (atom by atom) that is a patchwork of short shell
+  // runs.  Here the shells are ordered by cutoff radius (largest first), then
+  // by the Morton code of their centre, so a block's union becomes a few long
+  // runs per radius, and the P gather and the VXC atomics touch fewer DRAM
+  // sectors.  P_ and A_ live in this order; P comes in and VXC goes out
+  // through permuting copies.
+  const int nsh_all = (int)bs.shells.size();
+  std::vector<int> shell_pos(nsh_all), new_off(nsh_all), shell_at(nsh_all);
+  {
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (const auto& sh : bs.shells)
+      for (int k = 0; k < 3; ++k) {
+        lo[k] = std::min(lo[k], sh.O[k]);
+        hi[k] = std::max(hi[k], sh.O[k]);
+      }
+    auto morton = [&](const double* O) {
+      uint64_t code = 0;
+      for (int k = 0; k < 3; ++k) {
+        const double span = hi[k] - lo[k];
+        const uint64_t q = span > 0. ? (uint64_t)std::min(1023., (O[k] - lo[k]) / span * 1023.) : 0;
+        for (int bit = 0; bit < 10; ++bit) code |= ((q >> bit) & 1ull) << (3 * bit + k);
+      }
+      return code;
+    };
+    std::vector<uint64_t> mc(nsh_all);
+    for (int x = 0; x < nsh_all; ++x) mc[x] = morton(bs.shells[x].O);
+    std::vector<int> ord(nsh_all);
+    std::iota(ord.begin(), ord.end(), 0);
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
+      const Shell &sa = bs.shells[a], &sb = bs.shells[b];
+      if (sa.cutoff_radius != sb.cutoff_radius) return sa.cutoff_radius > sb.cutoff_radius;
+      if (sa.l != sb.l) return sa.l < sb.l;
+      return mc[a] < mc[b];
+    });
+    std::vector<int> perm(nbf_), iperm(nbf_);
+    int o = 0;
+    for (int k = 0; k < nsh_all; ++k) {
+      const int x = ord[k];
+      shell_pos[x] = k;
+      shell_at[k] = x;
+      new_off[x] = o;
+      for (int f = 0; f < bs.shells[x].size(); ++f) {
+        perm[o + f] = bs.shell_offs[x] + f;
+        iperm[bs.shell_offs[x] + f] = o + f;
+      }
+      o += bs.shells[x].size();
+    }
+    perm_ = arena_.upload(perm, s);
+    iperm_ = arena_.upload(iperm, s);
+  }
   // Task order of the merge: along a Morton curve of the tasks' centroids
   // (0.5 bohr cells, coarser when the molecule spans more than 511 bohr), so
   // that consecutive tasks are spatial neighbours and merged blocks stay
@@ -528,25 +581,25 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
   }
   // Merge: each task (piece) joins the cheapest of the last kMergeWindow
   // blocks with room for its points, if that does not raise the cost, else
-  // it opens a block.  The open blocks' shell sets are bitsets; the union's
+  // it opens a block.  The open blocks' shell sets are bitsets over the
+  // device AO order (so a closed block lists its shells in that order); the union's
   // basis size is nu(b) + nbe(t) - nbe(b & t), the intersection counted per
   // shell size class with popcounts.  On 256 waters (CPU model) the window of
   // 8 gives 40k blocks and 35 % less sum nu^2 than joining only the last
   // block, for 3 % less tensor work.
   constexpr int kMergeWindow = 8;
-  const int nsh_all = (int)bs.shells.size();
   const int nw = (nsh_all + 63) / 64;
   std::vector<int> csize;                     // distinct shell sizes
   std::vector<std::vector<uint64_t>> cmask;   // shells of each size, as bitsets
   for (int x = 0; x < nsh_all; ++x) {
-    const int sz = bs.shells[x].size();
+    const int sz = bs.shells[x].size(), q = shell_pos[x];
     size_t c = 0;
     while (c < csize.size() && csize[c] != sz) ++c;
     if (c == csize.size()) {
       csize.push_back(sz);
       cmask.emplace_back(nw, 0ull);
     }
-    cmask[c][x >> 6] |= 1ull << (x & 63);
+    cmask[c][q >> 6] |= 1ull << (q & 63);
   }
   auto common_nbe = [&](const std::vector<uint64_t>& a, const std::vector<uint64_t>& b) {
     int n = 0;
@@ -567,14 +620,15 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
     PB& b = pbs[win.front().pb];
     b.shells.clear();
     for (int i = 0; i < nw; ++i)
-      for (uint64_t w = win.front().bits[i]; w; w &= w - 1) b.shells.push_back(i * 64 + __builtin_ctzll(w));
+      for (uint64_t w = win.front().bits[i]; w; w &= w - 1)
+        b.shells.push_back(shell_at[i * 64 + __builtin_ctzll(w)]);
     win.erase(win.begin());
   };
   std::vector<uint64_t> tb(nw);
   for (int t : torder) {
     const XCTask& tt = tasks[t];
     std::fill(tb.begin(), tb.end(), 0ull);
-    for (int x : tt.shell_list) tb[x >> 6] |= 1ull << (x & 63);
+    for (int x : tt.shell_list) tb[shell_pos[x] >> 6] |= 1ull << (shell_pos[x] & 63);
     for (int p0 = 0; p0 < tt.npts; p0 += maxp) {
       const int p1 = std::min(tt.npts, p0 + maxp), n = p1 - p0;
       int best = -1, best_nu = 0;
@@ -616,56 +670,6 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
 
   timings["plan_merge_ms"] = ms_since(t_plan0);
   const auto t_layout0 = std::chrono::steady_clock::now();
-  // Device AO order.  A block's union basis holds, for every cutoff radius,
-  // the shells of that radius whose centres lie within reach of its points:
-  // in the caller's order (atom by atom) that is a patchwork of short shell
-  // runs.  Here the shells are ordered by cutoff radius (largest first), then
-  // by the Morton code of their centre, so a block's union becomes a few long
-  // runs per radius, and the P gather and the VXC atomics touch fewer DRAM
-  // sectors.  P_ and A_ live in this order; P comes in and VXC goes out
-  // through permuting copies.
-  std::vector<int> shell_pos(nsh_all), new_off(nsh_all);
-  {
-    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-    for (const auto& sh : bs.shells)
-      for (int k = 0; k < 3; ++k) {
-        lo[k] = std::min(lo[k], sh.O[k]);
-        hi[k] = std::max(hi[k], sh.O[k]);
-      }
-    auto morton = [&](const double* O) {
-      uint64_t code = 0;
-      for (int k = 0; k < 3; ++k) {
-        const double span = hi[k] - lo[k];
-        const uint64_t q = span > 0. ? (uint64_t)std::min(1023., (O[k] - lo[k]) / span * 1023.) : 0;
-        for (int bit = 0; bit < 10; ++bit) code |= ((q >> bit) & 1ull) << (3 * bit + k);
-      }
-      return code;
-    };
-    std::vector<uint64_t> mc(nsh_all);
-    for (int x = 0; x < nsh_all; ++x) mc[x] = morton(bs.shells[x].O);
-    std::vector<int> ord(nsh_all);
-    std::iota(ord.begin(), ord.end(), 0);
-    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
-      const Shell &sa = bs.shells[a], &sb = bs.shells[b];
-      if (sa.cutoff_radius != sb.cutoff_radius) return sa.cutoff_radius > sb.cutoff_radius;
-      if (sa.l != sb.l) return sa.l < sb.l;
-      return mc[a] < mc[b];
-    });
-    std::vector<int> perm(nbf_), iperm(nbf_);
-    int o = 0;
-    for (int k = 0; k < nsh_all; ++k) {
-      const int x = ord[k];
-      shell_pos[x] = k;
-      new_off[x] = o;
-      for (int f = 0; f < bs.shells[x].size(); ++f) {
-        perm[o + f] = bs.shell_offs[x] + f;
-        iperm[bs.shell_offs[x] + f] = o + f;
-      }
-      o += bs.shells[x].size();
-    }
-    perm_ = arena_.upload(perm, s);
-    iperm_ = arena_.upload(iperm, s);
-  }
 
   const int npb = (int)pbs.size();
   std::vector<int64_t> pt_off(npb), bf_off(npb), sh_off(npb), f64_off(npb), dig_off(npb),
@@ -673,10 +677,10 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
   std::vector<int> npts_pad(npb), nk(npb), nu(npb), nu_pad(npb), nsh(npb), bf_list, sh_list,
       sh_col, member;
   std::vector<uint8_t> mask;
-  std::vector<uint64_t> mbits(nw, 0ull);  // a member task's shells (cleared after use)
   std::vector<double> X, Y, Z, W;
   stats = PlanStats{};
-  int64_t pts = 0;
+  // pass 1 (sequential): sizes and offsets of every block's lists
+  int64_t pts = 0, nsh_tot = 0, nbf_tot = 0, nmask = 0;
   for (int i = 0; i < npb; ++i) {
     const PB& b = pbs[order[i]];
     pt_off[i] = pts;
@@ -685,50 +689,13 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
     nu[i] = b.nu;
     nu_pad[i] = (int)round_up(b.nu, kMTile);
     nsh[i] = (int)b.shells.size();
-    sh_off[i] = (int64_t)sh_list.size();
-    bf_off[i] = (int64_t)bf_list.size();
-    // the union's columns in device AO order (shell data stays indexed by
-    // the caller's shell index)
-    std::vector<int> ushells(b.shells);
-    std::sort(ushells.begin(), ushells.end(),
-              [&](int a, int c) { return shell_pos[a] < shell_pos[c]; });
-    int col = 0;
-    for (int x : ushells) {
-      sh_list.push_back(x);
-      sh_col.push_back(col);
-      for (int k = 0; k < bs.shells[x].size(); ++k) bf_list.push_back(new_off[x] + k);
-      col += bs.shells[x].size();
-    }
-    for (int k = col; k < nu_pad[i]; ++k) bf_list.push_back(-1);
-    mask_off[i] = (int64_t)mask.size();
-    for (size_t m = 0; m < b.segs.size(); ++m) {
-      const XCTask& tt = tasks[b.segs[m].task];
-      for (int x : tt.shell_list) mbits[x >> 6] |= 1ull << (x & 63);
-      for (int x : ushells) mask.push_back((uint8_t)((mbits[x >> 6] >> (x & 63)) & 1ull));
-      for (int x : tt.shell_list) mbits[x >> 6] = 0ull;
-    }
-    int np_real = 0;
-    for (size_t m = 0; m < b.segs.size(); ++m) {
-      const Seg& sg = b.segs[m];
-      const XCTask& tt = tasks[sg.task];
-      for (int p = sg.p0; p < sg.p1; ++p) {
-        X.push_back(tt.points[3 * p]);
-        Y.push_back(tt.points[3 * p + 1]);
-        Z.push_back(tt.points[3 * p + 2]);
-        W.push_back(tt.weights[p]);
-        member.push_back((int)m);
-        ++np_real;
-      }
-    }
-    for (int p = np_real; p < npts_pad[i]; ++p) {
-      X.push_back(X[pts]);
-      Y.push_back(Y[pts]);
-      Z.push_back(Z[pts]);
-      W.push_back(0.);
-      member.push_back(0);
-    }
+    sh_off[i] = nsh_tot;
+    bf_off[i] = nbf_tot;
+    mask_off[i] = nmask;
+    nsh_tot += nsh[i];
+    nbf_tot += nu_pad[i];
+    nmask += (int64_t)b.segs.size() * nsh[i];
     pts += npts_pad[i];
-    npts_plan_ = pts;
     stats.npts += b.npts;
     stats.sum_pad_npts_nbe2 += (double)npts_pad[i] * nu_pad[i] * nu_pad[i];
     {
@@ -746,6 +713,69 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
       stats.kbytes[2] += nq * phi + 32. * d.np + 12. * (double)(d.nu128 + d.nun) * d.nk;  // Z digits
       stats.kbytes[3] += 12. * (double)(d.nu128 + d.nun) * 2. * d.nk + 8. * d.nu * d.nu;  // VXC GEMM
     }
+  }
+  npts_plan_ = pts;
+  sh_list.resize(nsh_tot);
+  sh_col.resize(nsh_tot);
+  bf_list.resize(nbf_tot);
+  mask.resize(nmask);
+  X.resize(pts);
+  Y.resize(pts);
+  Z.resize(pts);
+  W.resize(pts);
+  member.resize(pts);
+  // pass 2 (host threads over blocks): the union's columns in device AO
+  // order (shell data stays indexed by the caller's shell index), each
+  // member task's shell mask over the union, and the points (padded with
+  // zero-weight copies of the block's first point)
+  auto fill = [&](int i0, int i1) {
+    std::vector<uint64_t> mbits(nw, 0ull);  // a member task's shells (cleared after use)
+    for (int i = i0; i < i1; ++i) {
+      const PB& b = pbs[order[i]];
+      const std::vector<int>& ushells = b.shells;
+      int64_t so = sh_off[i], bo = bf_off[i];
+      int col = 0;
+      for (int x : ushells) {
+        sh_list[so] = x;
+        sh_col[so++] = col;
+        for (int k = 0; k < bs.shells[x].size(); ++k) bf_list[bo++] = new_off[x] + k;
+        col += bs.shells[x].size();
+      }
+      for (int k = col; k < nu_pad[i]; ++k) bf_list[bo++] = -1;
+      int64_t mo = mask_off[i];
+      for (size_t m = 0; m < b.segs.size(); ++m) {
+        const XCTask& tt = tasks[b.segs[m].task];
+        for (int x : tt.shell_list) mbits[x >> 6] |= 1ull << (x & 63);
+        for (int x : ushells) mask[mo++] = (uint8_t)((mbits[x >> 6] >> (x & 63)) & 1ull);
+        for (int x : tt.shell_list) mbits[x >> 6] = 0ull;
+      }
+      int64_t g = pt_off[i];
+      for (size_t m = 0; m < b.segs.size(); ++m) {
+        const Seg& sg = b.segs[m];
+        const XCTask& tt = tasks[sg.task];
+        for (int p = sg.p0; p < sg.p1; ++p, ++g) {
+          X[g] = tt.points[3 * p];
+          Y[g] = tt.points[3 * p + 1];
+          Z[g] = tt.points[3 * p + 2];
+          W[g] = tt.weights[p];
+          member[g] = (int)m;
+        }
+      }
+      for (const int64_t g0 = pt_off[i]; g < pt_off[i] + npts_pad[i]; ++g) {
+        X[g] = X[g0];
+        Y[g] = Y[g0];
+        Z[g] = Z[g0];
+        W[g] = 0.;
+        member[g] = 0;
+      }
+    }
+  };
+  {
+    const int nthr = std::max(1, std::min<int>(32, (int)std::thread::hardware_concurrency()));
+    std::vector<std::thread> pool;
+    for (int k = 0; k < nthr; ++k)
+      pool.emplace_back(fill, (int)((int64_t)npb * k / nthr), (int)((int64_t)npb * (k + 1) / nthr));
+    for (auto& th : pool) th.join();
   }
   for (const auto& t : tasks) {
     stats.sum_npts_nbe += (double)t.npts * t.nbe;
