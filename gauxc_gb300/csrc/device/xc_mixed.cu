@@ -27,10 +27,11 @@ __device__ __forceinline__ int exp_of_pow2(double p) {
 
 // Digits of 8 values x[e] (|x[e]| < 2^es[e]; double or float-float) stored as
 // kSlices 16-byte rows: plane i at out + i * plane.
+// Digit planes of 8 values as BF16 pairs: w[i][k] holds digit i of x[2k]
+// (low half) and x[2k + 1] (high half).
 template <typename T>
-__device__ __forceinline__ void store_digits8(const T (&x)[8], const int (&es)[8],
-                                              __nv_bfloat16* out, int64_t plane) {
-  uint32_t w[kSlices][4];
+__device__ __forceinline__ void digits8(const T (&x)[8], const int (&es)[8],
+                                        uint32_t (&w)[kSlices][4]) {
 #pragma unroll
   for (int e = 0; e < 8; e += 2) {
     float a[kSlices];
@@ -38,9 +39,21 @@ __device__ __forceinline__ void store_digits8(const T (&x)[8], const int (&es)[8
     ff::digits_f32<kSlices>(ff::fixed42(x[e + 1], es[e + 1]),
                             [&](int i, float v) { w[i][e >> 1] = ff::pack_bf16x2(a[i], v); });
   }
+}
+
+__device__ __forceinline__ void store_planes(const uint32_t (&w)[kSlices][4], __nv_bfloat16* out,
+                                             int64_t plane) {
 #pragma unroll
   for (int i = 0; i < kSlices; ++i)
     __stcs(reinterpret_cast<uint4*>(out + i * plane), make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]));
+}
+
+template <typename T>
+__device__ __forceinline__ void store_digits8(const T (&x)[8], const int (&es)[8],
+                                              __nv_bfloat16* out, int64_t plane) {
+  uint32_t w[kSlices][4];
+  digits8(x, es, w);
+  store_planes(w, out, plane);
 }
 
 using ff::ffl;
@@ -119,8 +132,10 @@ __global__ void phi_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const doub
     }
 #pragma unroll
     for (int e = 0; e < 8; ++e) es[e] = exp_of_pow2(v.sp[p0 + e]);
-    store_digits8(x, es, v.Va + oz_offset(0, mu, p0, kMTile, k2), kMTile * kBK);
-    if (mu < d.nun) store_digits8(x, es, v.Vb + oz_offset(0, mu, d.nk + p0, kNTile, k2), kNTile * kBK);
+    uint32_t w[kSlices][4];  // one split for both operands
+    digits8(x, es, w);
+    store_planes(w, v.Va + oz_offset(0, mu, p0, kMTile, k2), kMTile * kBK);
+    if (mu < d.nun) store_planes(w, v.Vb + oz_offset(0, mu, d.nk + p0, kNTile, k2), kNTile * kBK);
   }
   // Fd: thread (point p, sub-lane sub) takes every nsub-th row group of this
   // CTA's share, so that small blocks keep all threads busy
@@ -293,8 +308,10 @@ __global__ void __launch_bounds__(256, 4) z_digits_kernel(TasksDev tk, MixedPBDe
   int es[8];
 #pragma unroll
   for (int e = 0; e < 8; ++e) es[e] = es_z;
-  store_digits8(x, es, v.Va + oz_offset(0, row, d.nk + g * 8, kMTile, k2), kMTile * kBK);
-  if (row < d.nun) store_digits8(x, es, v.Vb + oz_offset(0, row, g * 8, kNTile, k2), kNTile * kBK);
+  uint32_t w[kSlices][4];  // one split for both operands
+  digits8(x, es, w);
+  store_planes(w, v.Va + oz_offset(0, row, d.nk + g * 8, kMTile, k2), kMTile * kBK);
+  if (row < d.nun) store_planes(w, v.Vb + oz_offset(0, row, g * 8, kNTile, k2), kNTile * kBK);
 }
 
 // ---------------------------------------------------------------- functional
