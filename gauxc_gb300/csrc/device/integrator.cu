@@ -836,7 +836,7 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
     // consecutive slots, so each CTA sums a tile's chunks before the phi
     // contraction and the chains of one row block share their A blocks.
     {
-      const int nchunk = (d.nu16 + kMaxK - 1) / kMaxK;
+      const int nchunk = (d.nu16 + kMaxKX - 1) / kMaxKX;
       std::vector<std::pair<int, int>> ch;
       for (int m0 = 0; m0 < d.nu128; m0 += kMTile)
         for (int n0 = 0; n0 < d.np; n0 += kNTile) ch.push_back({m0, n0});
@@ -847,8 +847,8 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
               xi.push_back(OzItem{-1, 0, 0, 0, 0, 0, 0});
               continue;
             }
-            xi.push_back(OzItem{i, ch[c0 + r].first, ch[c0 + r].second, c * kMaxK,
-                                std::min((c + 1) * kMaxK, d.nu16), 0, 0});
+            xi.push_back(OzItem{i, ch[c0 + r].first, ch[c0 + r].second, c * kMaxKX,
+                                std::min((c + 1) * kMaxKX, d.nu16), 0, 0});
             oz_set_operands(xi.back(), d, dig_off[i], false);
           }
     }
