@@ -483,7 +483,7 @@ class XCIntegrator(_Handle):
         return st
 
 
-    def set_plan_params(self, pb_max_pts=256, nu2_weight=100.0, scratch_gb=0.0):
+    def set_plan_params(self, pb_max_pts=384, nu2_weight=100.0, scratch_gb=0.0):
         """Plan parameters (point-block size and merge weight of "GB300-Mixed",
         work-space cap in GB, 0 = from free memory); the plan is rebuilt on the
         next call."""

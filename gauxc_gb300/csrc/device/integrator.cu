@@ -836,7 +836,7 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
     // consecutive slots, so each CTA sums a tile's chunks before the phi
     // contraction and the chains of one row block share their A blocks.
     {
-      const int nchunk = (d.nu16 + kMaxKX - 1) / kMaxKX;
+      const int nchunk = (d.nu16 + kMaxK - 1) / kMaxK;
       std::vector<std::pair<int, int>> ch;
       for (int m0 = 0; m0 < d.nu128; m0 += kMTile)
         for (int n0 = 0; n0 < d.np; n0 += kNTile) ch.push_back({m0, n0});
@@ -847,8 +847,8 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
               xi.push_back(OzItem{-1, 0, 0, 0, 0, 0, 0});
               continue;
             }
-            xi.push_back(OzItem{i, ch[c0 + r].first, ch[c0 + r].second, c * kMaxKX,
-                                std::min((c + 1) * kMaxKX, d.nu16), 0, 0});
+            xi.push_back(OzItem{i, ch[c0 + r].first, ch[c0 + r].second, c * kMaxK,
+                                std::min((c + 1) * kMaxK, d.nu16), 0, 0});
             oz_set_operands(xi.back(), d, dig_off[i], false);
           }
     }
@@ -1406,7 +1406,7 @@ double integrator_autotune(XCIntegratorHandle& h, const double* P, int64_t ldp, 
   std::vector<double> V((size_t)nbf * nbf);
   std::vector<PlanParams> cands;
   if (h.prec == Precision::Mixed) {
-    for (int pts : {128, 192, 256})
+    for (int pts : {128, 256, 384})
       for (double w : {75., 150.}) cands.push_back(PlanParams{pts, w, h.params.scratch_bytes});
   } else {
     cands.push_back(h.params);

@@ -2,7 +2,7 @@
 // FP32 level accumulators in TMEM) with two fused epilogues:
 //
 //  X tile (density): D[nu, p] = sum_mu Pd[nu, mu] Fd[p, mu], K chunks of
-//    <= 768 (kMaxKX) run back to back on one CTA and are summed in float-float
+//    <= 768 (kMaxK) run back to back on one CTA and are summed in float-float
 //    registers; X'[nu, p] = 2 * 2^-14 * D * r_nu * s_p is then contracted
 //    with phi[nu, p] (rho) and 2 grad phi[nu, p] (grad rho); the sums over
 //    the tile's 128 basis rows (TMEM lanes) run as warp reduce-scatters in

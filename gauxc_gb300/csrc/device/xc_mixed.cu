@@ -108,9 +108,8 @@ __device__ __forceinline__ unsigned long long row8_max(unsigned long long m,
 // ---------------------------------------------------------------- phi digits
 // Va[mu][p] (K < nk) and Vb[mu][nk + p] (rows mu < nun): one thread per
 // (mu, 8 points), consecutive threads on consecutive mu.  Fd (rows p, K = mu):
-// thread p of the CTA walks the CTA's share of the basis in groups of 8
-// (kPBMaxPts <= blockDim.x).  The point scales sp come from the collocation
-// kernel.
+// the CTA's threads walk (point, group of 8 rows) items of the CTA's share of
+// the basis.  The point scales sp come from the collocation kernel.
 __global__ void phi_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const double* f64,
                                   __nv_bfloat16* dig, int gga) {
   const int b = b0 + blockIdx.y;
@@ -137,19 +136,18 @@ __global__ void phi_digits_kernel(TasksDev tk, MixedPBDev mp, int b0, const doub
     store_planes(w, v.Va + oz_offset(0, mu, p0, kMTile, k2), kMTile * kBK);
     if (mu < d.nun) store_planes(w, v.Vb + oz_offset(0, mu, d.nk + p0, kNTile, k2), kNTile * kBK);
   }
-  // Fd: thread (point p, sub-lane sub) takes every nsub-th row group of this
-  // CTA's share, so that small blocks keep all threads busy
-  const int nsub = blockDim.x / d.np, sub = threadIdx.x / d.np, p = threadIdx.x % d.np;
-  if (sub >= nsub) return;
+  // Fd: items (point p, group of 8 rows) of this CTA's share of the row
+  // groups, consecutive threads on consecutive points
   const int ng = d.nu16 / 8;
   const int per = (ng + gridDim.x - 1) / gridDim.x;
   const int g0 = blockIdx.x * per, g1 = min(ng, g0 + per);
-  int es[8];
-  const int e0 = exp_of_pow2(v.sp[p]);
+  const int nitems = d.np * max(g1 - g0, 0);
+  for (int item = threadIdx.x; item < nitems; item += blockDim.x) {
+    const int p = item % d.np, mu0 = (g0 + item / d.np) * 8;
+    int es[8];
+    const int e0 = exp_of_pow2(v.sp[p]);
 #pragma unroll
-  for (int e = 0; e < 8; ++e) es[e] = e0;
-  for (int g = g0 + sub; g < g1; g += nsub) {
-    const int mu0 = g * 8;
+    for (int e = 0; e < 8; ++e) es[e] = e0;
     ffl x[8];
 #pragma unroll
     for (int e = 0; e < 8; ++e) x[e] = v.phi[(int64_t)(mu0 + e) * d.np + p];

@@ -7,11 +7,10 @@
 // |d_i| <= 64 (i > 1).  Digit i is stored in BF16 as d_i 2^(-7 (i - 1)), which
 // is exact.  A product is the sum over slice pairs (i, j) with i + j <= kLevels
 // of BF16 GEMMs (21 pairs); pairs of equal i + j share one TMEM accumulator,
-// each an exact integer sum in FP32 for a K extent of at most 512 (the VXC
-// GEMM: 512 * 3 * 2^13 < 2^24); the density GEMM's chunks of 768 keep levels
-// 0-2 exact (kMaxKX).  The epilogue adds the six levels in float-float
-// arithmetic (the three smallest, 2^-21 of the result and below, first in
-// FP32).
+// levels 0-2 exact integer sums in FP32 for a K extent of at most 768
+// (kMaxK; levels 3-5, 2^-21 of the result and below, may round).  The
+// epilogue adds the six levels in float-float arithmetic (the three
+// smallest first in FP32).
 //
 // GEMM operands live in HBM already in the tensor core's shared-memory image:
 // tiles of TR rows (128 for the M operand, 64 for the N operand) by kBK
@@ -31,17 +30,17 @@ namespace gb300 {
 
 constexpr int kSlices = 6;      // digits per operand
 constexpr int kLevels = 7;      // keep pairs with i + j <= kLevels
-constexpr int kMaxK = 512;      // K extent of one tensor-core GEMM (exactness bound)
-// K extent of one density-GEMM chunk.  Level L sums K (L + 1) digit products,
-// at most 2^13 each with the leading digit (|d_0| <= 128) and 2^12 otherwise:
-// levels 0-2 stay below 20480 K, exact in FP32 for K <= 819.  Levels 3-5 may
-// round beyond K = 512, by 2^-24 of values below 2^-21 of the result
-// (2^-45, under the 2^-42 of the digits themselves).
-constexpr int kMaxKX = 768;
+// K extent of one tensor-core GEMM (a density chunk; the VXC GEMM's 2 nk).
+// Level L sums K (L + 1) digit products, at most 2^13 each with the leading
+// digit (|d_0| <= 128) and 2^12 otherwise: levels 0-2 stay below 20480 K,
+// exact in FP32 for K <= 819.  Levels 3-5 may round beyond K = 512, by 2^-24
+// of values below 2^-21 of the result (2^-45, under the 2^-42 of the digits
+// themselves).
+constexpr int kMaxK = 768;
 constexpr int kMTile = 128;     // rows of a GEMM tile (M operand)
 constexpr int kNTile = 64;      // columns of a GEMM tile (N operand rows)
 constexpr int kBK = 16;         // K extent of one operand tile (one MMA)
-constexpr int kPBMaxPts = 256;  // points per point block (2 x 256 = kMaxK for the VXC GEMM)
+constexpr int kPBMaxPts = 384;  // points per point block (2 x 384 = kMaxK for the VXC GEMM)
 
 __host__ __device__ constexpr int oz_round(int x, int m) { return (x + m - 1) / m * m; }
 

@@ -38,7 +38,7 @@ struct PlanStats {
 
 // Tunable parameters of the tensor-core plan (point blocks).
 struct PlanParams {
-  int pb_max_pts = 256;       // points per point block (multiple of 64, <= 256)
+  int pb_max_pts = 384;       // points per point block (multiple of 64, <= 384)
   double nu2_weight = 100.;   // merge-rule cost of one union-basis element squared
                               // (gather / scatter work per block), in tile MACs
   double scratch_bytes = 0.;  // cap of the per-pass work space (0 = from free memory);

@@ -320,7 +320,7 @@ int gauxc_gb300_host_register(GauXCStatus* status, void* ptr, size_t bytes);
 void gauxc_gb300_host_unregister(GauXCStatus* status, void* ptr);
 /* Self-test of the tensor-core (split-mantissa BF16) VXC GEMM: the symmetric
    n x n product F Z^T + Z F^T over k points (n multiple of 128, k multiple of
-   64, k <= 256) against FP64; returns the worst error relative to the largest
+   64, k <= 384) against FP64; returns the worst error relative to the largest
    output element. */
 double gauxc_gb300_tensor_core_selftest(GauXCStatus* status, int n, int k);
 /* Self-test of the float-float exp of the tensor-core path's collocation:
@@ -365,14 +365,14 @@ void gauxc_gb300_collocation(GauXCStatus* status, const GauXCBasisSet basis, int
    the per-member work is gauxc_integrator_eval_exc_vxc_rks, xc_integrator.h:180) */
 
 /* Plan parameters: points per point block of a "GB300-Mixed" integrator
-   (multiple of 64, 64..256), the weight of a block's union-basis gather and
+   (multiple of 64, 64..384), the weight of a block's union-basis gather and
    scatter work in the block-merge rule, and a cap (GB, 0 = from free memory)
    on the device work space of one pass over the grid; a plan needing more
    runs in several passes.  The plan is rebuilt on the next call. */
 void gauxc_gb300_integrator_set_plan_params(GauXCStatus* status, const GauXCIntegrator integrator,
                                             int pb_max_pts, double nu2_weight, double scratch_gb);
 /* Autotuner: builds and times one call per candidate plan (point-block sizes
-   128/192/256 x merge weights 75/150 for "GB300-Mixed"; the current plan
+   128/256/384 x merge weights 75/150 for "GB300-Mixed"; the current plan
    otherwise) on density P and keeps the fastest.  Returns its compute time in
    ms and the chosen parameters. */
 double gauxc_gb300_integrator_autotune(GauXCStatus* status, const GauXCIntegrator integrator,

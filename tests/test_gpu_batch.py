@@ -87,7 +87,7 @@ def test_autotune_keeps_results(g, members):
     r = members[-1]
     ms, params = r["imx"].autotune(r["P"])
     assert ms > 0.
-    assert params["pb_max_pts"] in (128, 192, 256)
+    assert params["pb_max_pts"] in (128, 256, 384)
     assert params["nu2_weight"] in (75.0, 150.0)
     e, v = r["imx"].eval_exc_vxc(r["P"])
     assert abs(e - r["e64"]) <= TOL_MIXED
