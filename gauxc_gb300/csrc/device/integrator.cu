@@ -582,11 +582,11 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
   // Merge: each task (piece) joins the cheapest of the last kMergeWindow
   // blocks with room for its points, if that does not raise the cost, else
   // it opens a block.  The open blocks' shell sets are bitsets over the
-  // device AO order (so a closed block lists its shells in that order); the union's
-  // basis size is nu(b) + nbe(t) - nbe(b & t), the intersection counted per
-  // shell size class with popcounts.  On 256 waters (CPU model) the window of
-  // 8 gives 40k blocks and 35 % less sum nu^2 than joining only the last
-  // block, for 3 % less tensor work.
+  // device AO order (so a closed block lists its shells in that order); the
+  // union's basis size is nu(b) + nbe(t) - nbe(b & t), the intersection
+  // counted per shell size class with popcounts.  On 256 waters (CPU model)
+  // the window of 8 gives 40k blocks and 35 % less sum nu^2 than joining only
+  // the last block, for 3 % less tensor work.
   constexpr int kMergeWindow = 8;
   const int nw = (nsh_all + 63) / 64;
   std::vector<int> csize;                     // distinct shell sizes
