@@ -22,9 +22,11 @@ call copies P in, runs the whole XC pass and copies VXC out.
             (host->device copy, XC pass, device->host copy, synchronize)
 --impl reference times the CPU restatement of the reference host integrator
 (oracle/: per-task collocation, BLAS dgemm / dsyr2k contractions as in the
-reference host driver, OpenMP over tasks on all host cores) on a fixed
-strided sample of the same tasks, extrapolated to one full iteration by the
-sample's share of sum npts*nbe^2 (the contractions' work).
+reference host driver, OpenMP over tasks on all host cores, tasks in the
+reference's npts*nbe order) on a fixed strided sample of the same tasks (the
+same sample as the cpu_baseline leg of the default arm), extrapolated to one
+full iteration: the per-call fixed cost (VXC zeroing and symmetrization) once,
+the rest by the sample's share of sum npts*nbe^2 (the contractions' work).
 """
 import argparse
 import json
@@ -240,18 +242,32 @@ def eval_into(integ, P, V):
 
 
 # ---------------------------------------------------------------------- CPU baseline
-def cpu_sample(infos, target_frac):
-    """Deterministic strided sample of the tasks (reference order: npts*nbe desc)."""
-    order = sorted(range(len(infos)), key=lambda i: -infos[i]["npts"] * infos[i]["nbe"])
-    stride = max(1, int(round(1.0 / target_frac)))
-    pick = sorted(order[::stride])
+# sum npts*nbe^2 of the timed sample: about 7 s of oracle work on 16
+# Neoverse-V2 cores; a workload holding less is timed in full
+CPU_SAMPLE_WORK = 3.0e11
+
+
+def cpu_sample(infos, work=CPU_SAMPLE_WORK):
+    """Deterministic stratified sample of the tasks holding about `work` of
+    sum npts*nbe^2: one task of every k in the reference's order (npts*nbe
+    descending), listed in that order; all tasks when the workload holds
+    less.  Returns (task indices, their share of sum npts*nbe^2, k)."""
+    order = sorted(range(len(infos)), key=lambda i: (-infos[i]["npts"] * infos[i]["nbe"], i))
     cost = np.array([infos[i]["npts"] * infos[i]["nbe"] ** 2 for i in range(len(infos))], float)
-    return pick, cost[pick].sum() / cost.sum()
+    total = cost.sum()
+    stride = 1 if work >= total else max(1, int(round(total / work)))
+    # one task from each run of `stride` consecutive tasks, at a seeded offset:
+    # a fixed offset would alias with the molecule's repeat (equal tasks of
+    # equivalent atoms sit side by side), so that the sample revisits a few
+    # atoms' P and VXC blocks, which the full pass never does
+    off = np.random.default_rng(stride).integers(0, stride, -(-len(order) // stride))
+    pick = [order[b * stride + o] for b, o in enumerate(off) if b * stride + o < len(order)]
+    return pick, cost[pick].sum() / total, stride
 
 
 class WeightedSample:
-    """Tasks of a strided sample with SSF weights from the oracle (host
-    algorithm), computed once for the sampled points only."""
+    """Tasks of a sample with SSF weights from the oracle (host algorithm),
+    computed once for the sampled points only."""
 
     def __init__(self, lb, coords, pick):
         import oracle
@@ -264,36 +280,58 @@ class WeightedSample:
             self.tasks.append((t["points"], w, t["shell_list"]))
 
 
-def choose_sample(infos, ob, lb, coords, P, func, budget_s):
-    """Grows a strided sample until one oracle pass takes >= budget_s / 2."""
-    import oracle
-    frac = 1.0 / 1024
-    while True:
-        pick, share = cpu_sample(infos, frac)
-        ws = WeightedSample(lb, coords, pick)
-        t0 = time.perf_counter()
-        oracle.eval_exc_vxc(ob, ws.tasks, P, func)
-        dt = time.perf_counter() - t0
-        if dt >= budget_s / 2 or frac >= 1.0:
-            return ws, pick, share, dt
-        frac = min(1.0, frac * max(2.0, min(8.0, (budget_s / 2) / max(dt, 1e-3))))
-
-
 def oracle_basis(basis):
     import oracle
     l, pure, nprim, alpha, coeff, origin, _ = basis.arrays()
     return oracle.Basis(l, pure, nprim, alpha, coeff, origin)
 
 
-def cpu_leg(basis, lb, mol, P, func, budget_s, infos=None):
-    """One bounded oracle sample of the workload, extrapolated."""
+def cpu_leg(basis, lb, mol, P, func, work=CPU_SAMPLE_WORK, infos=None):
+    """One oracle pass over a bounded sample of the workload, after a warm-up
+    pass, extrapolated to the full task list.  The per-call cost that does
+    not depend on the tasks (VXC zeroing and symmetrization over nbf^2,
+    argument marshalling), timed as a call on no tasks, counts once; the
+    rest scales by the sample's share of sum npts*nbe^2."""
     import oracle
     if infos is None:
         infos = [lb.task_info(i) for i in range(lb.ntasks())]
     ob = oracle_basis(basis)
-    ws, pick, share, dt = choose_sample(infos, ob, lb, mol.coords(), P, func, budget_s)
-    return dict(ws=ws, ob=ob, pick=pick, share=share, dt=dt, est=dt / share,
-                blas=oracle.blas_active())
+    pick, share, stride = cpu_sample(infos, work)
+    ws = WeightedSample(lb, mol.coords(), pick)
+    fixed = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        oracle.eval_exc_vxc(ob, [], P, func)
+        fixed.append(time.perf_counter() - t0)
+    leg = dict(ws=ws, ob=ob, pick=pick, share=float(share), stride=stride, fixed=min(fixed),
+               ntasks=len(infos), blas=oracle.blas_active())
+    oracle.eval_exc_vxc(ob, ws.tasks, P, func)
+    t0 = time.perf_counter()
+    oracle.eval_exc_vxc(ob, ws.tasks, P, func)
+    leg["dt"] = time.perf_counter() - t0
+    leg["est"] = extrapolate(leg, leg["dt"])
+    return leg
+
+
+def extrapolate(leg, dt):
+    """Full-iteration estimate from one timed pass over the leg's sample."""
+    return leg["fixed"] + max(dt - leg["fixed"], 0.0) / leg["share"]
+
+
+def cpu_baseline_dict(leg, value, cores, sample, extrapolated):
+    """The line's cpu_baseline object (plain JSON types)."""
+    return dict(value=float(value), unit="s", cores=int(cores), kind="port", cpu=cpu_model(),
+                blas=bool(leg["blas"]), sample=sample, extrapolated=bool(extrapolated))
+
+
+def sample_note(leg, dt):
+    if leg["share"] >= 1.0:
+        return f"all {leg['ntasks']} tasks (npts*nbe order, as the reference runs them), {dt:.2f} s"
+    return (f"{len(leg['pick'])} of {leg['ntasks']} tasks (one of every {leg['stride']} in the "
+            f"reference's npts*nbe order, run in that order) = {leg['share']:.4f} of sum "
+            f"npts*nbe^2, {dt:.2f} s per pass after a warm-up pass; the per-call fixed cost "
+            f"{leg['fixed']:.2f} s (VXC zeroing and symmetrization) counted once, the rest "
+            f"extrapolated by that share")
 
 
 # ---------------------------------------------------------------------- reference arm
@@ -317,29 +355,25 @@ def run_reference(args, ncores):
     k = int(np.argmax(costs))
     scale = sum(costs) / costs[k]
     sd, mol, basis, mg, lb = built[k]
-    leg = cpu_leg(basis, lb, mol, sd["P"], sd["functional"], args.cpu_budget / 2, all_infos[k])
-    times = []
+    leg = cpu_leg(basis, lb, mol, sd["P"], sd["functional"], args.cpu_work, all_infos[k])
+    times, dts = [], []
     for it in range(args.warmup + args.steps):
         t0 = time.perf_counter()
         oracle.eval_exc_vxc(leg["ob"], leg["ws"].tasks, sd["P"], sd["functional"])
         dt = time.perf_counter() - t0
         if it >= args.warmup:
-            times.append(dt / leg["share"] * scale)
+            dts.append(dt)
+            times.append(extrapolate(leg, dt) * scale)
     v = float(np.mean(times))
-    sample = (f"{len(leg['pick'])} of {len(all_infos[k])} tasks of the "
-              f"{'largest member' if len(built) > 1 else 'system'} (every "
-              f"{max(1, round(len(all_infos[k]) / max(len(leg['pick']), 1)))}th in npts*nbe order) = "
-              f"{leg['share']:.4f} of its sum npts*nbe^2, {np.mean(times) * leg['share'] / scale:.2f} s "
-              f"per step, extrapolated by that share" + (f" and x{scale:.2f} for all members"
-                                                          if len(built) > 1 else ""))
+    sample = (("largest member: " if len(built) > 1 else "") + sample_note(leg, float(np.mean(dts)))
+              + (f", x{scale:.2f} for all members by sum npts*nbe^2" if len(built) > 1 else ""))
     line = dict(metric=METRIC, value=v, unit="s", n_gpus=args.gpus, steps=args.steps,
                 warmup=args.warmup, ms_per_step=v * 1e3, higher_is_better=False,
                 scaling="weak", vs_baseline=None, dtype="f64",
                 data="synthetic: seeded water clusters, even-tempered basis, P=CC^T (no dataset)",
                 config=config_dict(args.config, stats, nbfs), impl="reference",
-                cpu_baseline=dict(value=v, unit="s", cores=ncores, kind="port",
-                                  cpu=cpu_model(), blas=bool(leg["blas"]), sample=sample,
-                                  extrapolated=True),
+                cpu_baseline=cpu_baseline_dict(leg, v, ncores, sample,
+                                               leg["share"] < 1.0 or len(built) > 1),
                 e2e=dict(value=v, unit="s", h2d_bytes_per_step=0, d2h_bytes_per_step=0))
     print(json.dumps(line), flush=True)
     return 0
@@ -477,13 +511,13 @@ def run_batched(args, ncores):
     if not args.no_cpu_baseline:
         k = int(np.argmax([st["sum_npts_nbe2"] for st in stats]))
         s, mol, basis, mg, lb = systems[k]
-        leg = cpu_leg(basis, lb, mol, s["P"], s["functional"], args.cpu_budget)
+        leg = cpu_leg(basis, lb, mol, s["P"], s["functional"], args.cpu_work)
         scale = s2 / stats[k]["sum_npts_nbe2"]
-        cpu = dict(value=leg["est"] * scale, unit="s", cores=os.cpu_count() or 1, kind="port",
-                   cpu=cpu_model(), blas=bool(leg["blas"]),
-                   sample=f"{len(leg['pick'])} tasks of the largest cluster ({leg['share']:.4f} "
-                          f"of its sum npts*nbe^2, {leg['dt']:.1f} s), scaled to all "
-                          f"{len(systems)} clusters by sum npts*nbe^2", extrapolated=True)
+        cpu = cpu_baseline_dict(
+            leg, leg["est"] * scale, os.cpu_count() or 1,
+            "largest cluster: " + sample_note(leg, leg["dt"])
+            + f", x{scale:.2f} for all {len(systems)} clusters by sum npts*nbe^2",
+            leg["share"] < 1.0 or len(systems) > 1)
     line = dict(
         metric=METRIC, value=value, unit="s", n_gpus=1, steps=args.steps,
         warmup=args.warmup, ms_per_step=value * 1e3, higher_is_better=False, scaling="weak",
@@ -513,7 +547,8 @@ def main():
     # with the FP64 device path timed beside it for the speed-up and the errors
     ap.add_argument("--config", type=int, default=4)
     ap.add_argument("--lwd", default="GB300-Mixed")
-    ap.add_argument("--cpu-budget", type=float, default=16.0)
+    ap.add_argument("--cpu-work", type=float, default=CPU_SAMPLE_WORK,
+                    help="CPU legs: sum npts*nbe^2 of the timed task sample")
     ap.add_argument("--scratch-gb", type=float, default=0.0,
                     help="cap of the plan's work space per pass (0 = from free memory)")
     ap.add_argument("--atom-stride", type=int, default=1,
@@ -667,12 +702,9 @@ def main():
     cpu = None
     if not args.no_cpu_baseline:
         leg = cpu_leg(ctx["basis"], ctx["lb"], ctx["mol"], s["P"], s["functional"],
-                      args.cpu_budget)
-        cpu = dict(value=leg["est"], unit="s", cores=ncores, kind="port", cpu=cpu_model(),
-                   blas=bool(leg["blas"]),
-                   sample=f"{len(leg['pick'])} of {int(stats['ntasks'])} tasks (strided over the "
-                          f"npts*nbe order) = {leg['share']:.4f} of sum npts*nbe^2, "
-                          f"{leg['dt']:.1f} s, extrapolated by that share", extrapolated=True)
+                      args.cpu_work)
+        cpu = cpu_baseline_dict(leg, leg["est"], ncores, sample_note(leg, leg["dt"]),
+                                leg["share"] < 1.0)
 
     nel = integ.last_nel()
     batched = None

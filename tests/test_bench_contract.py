@@ -25,3 +25,29 @@ def test_reference_arm_json_line():
     assert d["cpu_baseline"]["kind"] in ("port", "reference")
     assert d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+
+
+def test_cpu_leg_sample_and_json():
+    """The default arm's cpu_baseline leg: a stratified sample in the
+    reference's task order whose estimate and JSON object are well formed,
+    and a workload below the sample size timed in full."""
+    sys.path.insert(0, ROOT)
+    import bench
+    from gauxc_gb300 import workloads as W
+    sd = W.config(0)["systems"][0]
+    mol, basis, mg, lb = W.build_system(sd, device=False)
+    _, infos = bench.host_stats(lb)
+    total = sum(i["npts"] * i["nbe"] ** 2 for i in infos)
+    pick, share, stride = bench.cpu_sample(infos, total / 4)
+    assert stride == 4 and len(set(pick)) == len(pick)
+    keys = [infos[i]["npts"] * infos[i]["nbe"] for i in pick]
+    assert keys == sorted(keys, reverse=True)
+    assert 0.1 < share < 0.5
+    assert bench.cpu_sample(infos, total / 4)[0] == pick
+    for work, full in ((total / 4, False), (bench.CPU_SAMPLE_WORK, True)):
+        leg = bench.cpu_leg(basis, lb, mol, sd["P"], sd["functional"], work, infos)
+        assert (leg["share"] >= 1.0) == full
+        assert leg["est"] >= leg["dt"] > 0 and leg["fixed"] >= 0
+        d = bench.cpu_baseline_dict(leg, leg["est"], 1, bench.sample_note(leg, leg["dt"]),
+                                    leg["share"] < 1.0)
+        assert json.loads(json.dumps(d))["extrapolated"] is (not full)
