@@ -142,27 +142,34 @@ std::shared_ptr<LoadBalancer> make_load_balancer(std::shared_ptr<const Molecule>
       per_atom[iat].swap(kept);
     });
   }
-  std::vector<XCTask> tasks;
-  for (auto& v : per_atom)
-    for (auto& t : v) tasks.push_back(std::move(t));
-
-  std::stable_sort(tasks.begin(), tasks.end(), [](const XCTask& a, const XCTask& b) {
-    if (a.iParent != b.iParent) return a.iParent < b.iParent;
-    return a.shell_list < b.shell_list;
-  });
-
-  std::vector<XCTask> merged;
-  for (auto& t : tasks) {
-    if (!merged.empty() && merged.back().iParent == t.iParent &&
-        merged.back().shell_list == t.shell_list) {
-      XCTask& m = merged.back();
-      m.points.insert(m.points.end(), t.points.begin(), t.points.end());
-      m.weights.insert(m.weights.end(), t.weights.begin(), t.weights.end());
-      m.npts += t.npts;
-    } else {
-      merged.push_back(std::move(t));
+  // Sort each atom's tasks by shell list and merge equal lists (their points
+  // joined in batch order), atoms in parallel: every task of a list has one
+  // parent, so this is the global stable sort by (iParent, shell_list) and
+  // merge of the Default load balancer, done per parent.
+  parallel_atoms([&](size_t iat) {
+    std::vector<XCTask>& v = per_atom[iat];
+    std::stable_sort(v.begin(), v.end(), [](const XCTask& a, const XCTask& b) {
+      return a.shell_list < b.shell_list;
+    });
+    std::vector<XCTask> merged;
+    for (auto& t : v) {
+      if (!merged.empty() && merged.back().shell_list == t.shell_list) {
+        XCTask& m = merged.back();
+        m.points.insert(m.points.end(), t.points.begin(), t.points.end());
+        m.weights.insert(m.weights.end(), t.weights.begin(), t.weights.end());
+        m.npts += t.npts;
+      } else {
+        merged.push_back(std::move(t));
+      }
     }
-  }
+    v.swap(merged);
+  });
+  size_t ntask = 0;
+  for (const auto& v : per_atom) ntask += v.size();
+  std::vector<XCTask> merged;
+  merged.reserve(ntask);
+  for (auto& v : per_atom)
+    for (auto& t : v) merged.push_back(std::move(t));
   lb->tasks = std::move(merged);
   lb->generation++;
   return lb;
