@@ -601,12 +601,17 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
     }
     cmask[c][q >> 6] |= 1ull << (q & 63);
   }
-  auto common_nbe = [&](const std::vector<uint64_t>& a, const std::vector<uint64_t>& b) {
+  // basis functions of a block's shell set (bits a) shared with the current
+  // task, whose nonzero words tw hold its shells split by size class (tcb,
+  // csize.size() words per entry of tw)
+  std::vector<int> tw;
+  std::vector<uint64_t> tcb;
+  auto common_nbe = [&](const std::vector<uint64_t>& a) {
+    const size_t ncs = csize.size();
     int n = 0;
-    for (size_t c = 0; c < csize.size(); ++c) {
-      int k = 0;
-      for (int i = 0; i < nw; ++i) k += __builtin_popcountll(a[i] & b[i] & cmask[c][i]);
-      n += k * csize[c];
+    for (size_t j = 0; j < tw.size(); ++j) {
+      const uint64_t m = a[tw[j]];
+      for (size_t c = 0; c < ncs; ++c) n += __builtin_popcountll(m & tcb[j * ncs + c]) * csize[c];
     }
     return n;
   };
@@ -629,6 +634,13 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
     const XCTask& tt = tasks[t];
     std::fill(tb.begin(), tb.end(), 0ull);
     for (int x : tt.shell_list) tb[shell_pos[x] >> 6] |= 1ull << (shell_pos[x] & 63);
+    tw.clear();
+    tcb.clear();
+    for (int i = 0; i < nw; ++i)
+      if (tb[i]) {
+        tw.push_back(i);
+        for (size_t c = 0; c < csize.size(); ++c) tcb.push_back(tb[i] & cmask[c][i]);
+      }
     for (int p0 = 0; p0 < tt.npts; p0 += maxp) {
       const int p1 = std::min(tt.npts, p0 + maxp), n = p1 - p0;
       int best = -1, best_nu = 0;
@@ -636,7 +648,7 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
       for (int w = (int)win.size() - 1; w >= 0; --w) {
         const PB& b = pbs[win[w].pb];
         if (b.npts + n > maxp) continue;
-        const int nu = b.nu + tt.nbe - common_nbe(win[w].bits, tb);
+        const int nu = b.nu + tt.nbe - common_nbe(win[w].bits);
         const double d = pb_cost(b.npts + n, nu, w2) - pb_cost(b.npts, b.nu, w2) - pb_cost(n, tt.nbe, w2);
         if (d <= best_d) {
           best = w;
@@ -646,7 +658,7 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
       }
       if (best >= 0) {
         PB& b = pbs[win[best].pb];
-        for (int i = 0; i < nw; ++i) win[best].bits[i] |= tb[i];
+        for (int i : tw) win[best].bits[i] |= tb[i];
         b.nu = best_nu;
         b.npts += n;
         b.segs.push_back({t, p0, p1});
@@ -689,6 +701,11 @@ void DeviceIntegrator::build_mixed(const LoadBalancer& lb) {
     nu[i] = b.nu;
     nu_pad[i] = (int)round_up(b.nu, kMTile);
     nsh[i] = (int)b.shells.size();
+    {
+      int nu_shells = 0;  // the merge's running union size against the closed shell list
+      for (int x : b.shells) nu_shells += bs.shells[x].size();
+      if (nu_shells != b.nu) throw error("plan: point-block basis size disagrees with its shells");
+    }
     sh_off[i] = nsh_tot;
     bf_off[i] = nbf_tot;
     mask_off[i] = nmask;
